@@ -1,0 +1,244 @@
+"""Generate golden vectors by running the reference implementation itself.
+
+Run in a container where the reference checkout is mounted (it is read-only
+and never needed at test time):
+
+    python tests/golden/make_golden.py /path/to/bp_project
+
+The reference's CPU path is ``fast_bp/ffbp.py`` (Numba) and its FP64 planner
+is ``fast_bp/gpu_backend.py:build_ffbp_plan``.  Numba and CuPy are not
+installed here, so a no-op ``numba`` module (``njit`` returns the function,
+``prange`` is ``range``) and an empty ``cupy`` module are placed in
+``sys.modules`` first; the reference code then runs unchanged as pure
+Python.  The outputs are stored as small compressed ``.npz`` fixtures next
+to this script; tests compare the CPU oracle and the GPU path against them.
+
+Cases
+-----
+operator_validation.npz
+    The reference's GPU operator-validation recipe
+    (``fast_bp/gpu_baseline.py:121-187``, seed 20260916): 31 pulses x 512
+    random complex samples, leaf 8, both signs of k and both look sides,
+    Hann weights and a phase ramp.  Stores inputs, the reference FFBP image
+    (``form_ffbp``) and the reference direct image (``bp_polar`` on the plan
+    grid), plus the flattened plan.
+points.npz
+    A reduced ``fast_bp/validate.py`` scene (analytic sinc point targets on
+    a non-uniform 3-D track): ``backproject_points`` on point clusters,
+    ``form_ffbp`` + ``evaluate_image``, and ``target_contributions``.
+kernels.npz
+    ``regrid`` of a random polar image, ``sample1`` / ``sample2`` /
+    ``cubic_weights`` at random coordinates (including out-of-support ones).
+plans.npz
+    ``build_ffbp_plan`` on the benchmark trajectories (1024 pulses / leaf 64
+    and 4096 pulses / leaf 16) and on the validate.py track, flattened.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def import_reference(root: Path):
+    nb = types.ModuleType("numba")
+
+    def njit(*args, **kwargs):
+        if args and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda fn: fn
+
+    nb.njit = njit
+    nb.prange = range
+    nb.set_num_threads = lambda n: None
+    sys.modules["numba"] = nb
+    cp = types.ModuleType("cupy")
+    cp.ndarray = object
+    sys.modules["cupy"] = cp
+    os.environ.setdefault("FAST_BP_CUDA_ROOT", "/usr/local/cuda" if Path("/usr/local/cuda").exists() else str(root))
+    sys.path.insert(0, str(root / "fast_bp"))
+    import ffbp  # noqa: E402
+    import gpu_backend  # noqa: E402
+    return ffbp, gpu_backend
+
+
+def flatten_plan(plan):
+    """Pre-order node arrays of a reference FFBPPlan."""
+    nodes = []
+
+    def walk(n):
+        nodes.append(n)
+        if n.left is not None:
+            walk(n.left)
+            walk(n.right)
+
+    walk(plan.root)
+    nodes.sort(key=lambda n: n.index)
+    geom = np.array([[*n.origin, n.r0, n.dr, n.u0, n.du, n.side] for n in nodes], np.float64)
+    idx = np.array([[n.a, n.b, n.nr, n.nu, -1 if n.left is None else n.left.index,
+                     -1 if n.right is None else n.right.index] for n in nodes], np.int64)
+    crop = np.array([*plan.crop_r, *plan.crop_u], np.int64)
+    counts = np.array([plan.counts[k] for k in ("leaves", "merges", "leaf_pixel_pulse_products",
+                                                 "merged_pixels", "nodes")], np.int64)
+    root = np.array([plan.r0, plan.dr, plan.u0, plan.du, plan.nr, plan.nu], np.float64)
+    return geom, idx, crop, counts, root
+
+
+def operator_validation(ffbp, gb):
+    from scipy.signal.windows import hann
+    C, FC = 299792458.0, 1.4e9
+    rng = np.random.default_rng(20260916)
+    out = {}
+    for case, (sign, side) in enumerate(((-1, 1), (1, -1))):
+        pulses, samples = 31, 512
+        slow = np.arange(pulses, dtype=np.float64)
+        position = np.column_stack([0.05 * np.sin(0.37 * slow),
+                                    np.linspace(-15.0, 15.0, pulses) + 0.03 * np.sin(slow),
+                                    18.0 + 0.1 * np.cos(0.23 * slow)])
+        data = (rng.standard_normal((pulses, samples)) + 1j * rng.standard_normal((pulses, samples))).astype(np.complex64)
+        weight = hann(pulses)
+        phase = np.linspace(-0.2, 0.3, pulses)
+        range_start, data_dr = 900.0, 0.5
+        extent = (1080.0, 1120.0, -0.05, 0.05)
+        fc = sign * FC
+        k = 4.0 * np.pi * fc / C
+        plan = gb.build_ffbp_plan(position, fc, extent, side=side, leaf_size=8, range_spacing=0.5,
+                                  angular_oversample=3.0)
+        img, counts = ffbp.form_ffbp(data, position, range_start, data_dr, fc, extent, side=side, leaf_size=8,
+                                     range_spacing=0.5, angular_oversample=3.0, weight=weight, phase=phase,
+                                     verbose=False)
+        direct = ffbp.bp_polar(data, position, plan.origin, plan.r0, plan.dr, plan.nr, plan.u0, plan.du,
+                               plan.nu, range_start, data_dr, k, weight, phase, side)
+        geom, idx, crop, cnt, root = flatten_plan(plan)
+        p = f"case{case}_"
+        out.update({p + "data": data, p + "position": position, p + "weight": weight, p + "phase": phase,
+                    p + "scalars": np.array([range_start, data_dr, fc, k, side, *extent]),
+                    p + "ffbp": img.image, p + "ffbp_axes": np.array([*img.origin, img.r0, img.dr, img.u0, img.du]),
+                    p + "direct": direct, p + "geom": geom, p + "idx": idx, p + "crop": crop,
+                    p + "counts": cnt, p + "root": root})
+        print(f"operator case {case}: plan {plan.shape}, ffbp peak "
+              f"{np.unravel_index(np.abs(img.image).argmax(), img.image.shape)}, direct peak "
+              f"{np.unravel_index(np.abs(direct).argmax(), direct.shape)}", flush=True)
+    return out
+
+
+def validate_track(n):
+    t = np.linspace(-1, 1, n)
+    return np.column_stack([0.08 * np.sin(5 * t), 50 * t + 0.4 * t * t, 18 + 0.15 * np.sin(2 * t)])
+
+
+def points_case(ffbp):
+    from scipy.signal.windows import hann
+    C, FC, FS = 299792458.0, 1.4e9, 400e6
+    k = 4 * np.pi * FC / C
+    n = 64
+    pos = validate_track(n)
+    targets = np.array([[710.31, -145.27, 0.0], [987.21, 31.72, 0.0]])
+    strength = np.array([1, complex(0.7, 0.3)])
+    r_start, ddr = 500.0, C / (2 * FS)
+    rr = r_start + ddr * np.arange(1500)
+    data = np.zeros((n, len(rr)), np.complex64)
+    for xyz, a in zip(targets, strength):
+        distance = np.linalg.norm(pos - xyz, axis=1)
+        data += (a * np.exp(-1j * k * distance)[:, None]
+                 * np.sinc((rr[None, :] - distance[:, None]) / (C / (2 * 200e6)))).astype(np.complex64)
+    w = hann(n)
+    phase = np.zeros(n)
+    clusters = []
+    for xyz in targets:
+        x = xyz[0] + np.arange(-3, 3.01, 0.6)
+        y = xyz[1] + np.arange(-8, 8.01, 0.8)
+        xx, yy = np.meshgrid(x, y)
+        clusters.append(np.column_stack([xx.ravel(), yy.ravel(), np.zeros(xx.size)]))
+    points = np.vstack(clusters)
+    direct = ffbp.backproject_points(data, pos, points, r_start, ddr, k, w, phase)
+    extent = (718.0, 732.0, -0.215, -0.185)
+    img, counts = ffbp.form_ffbp(data, pos, r_start, ddr, FC, extent, leaf_size=32, range_spacing=0.5,
+                                 angular_oversample=2.0, weight=w, verbose=False)
+    cl = clusters[0]
+    fast = ffbp.evaluate_image(img.image, img.origin, img.r0, img.dr, img.u0, img.du, cl, k)
+    contrib = ffbp.target_contributions(data, pos, targets, r_start, ddr, k)
+    print(f"points: {len(points)} points, ffbp {img.image.shape}, counts {counts}", flush=True)
+    return {"data": data, "position": pos, "weight": w, "phase": phase, "points": points,
+            "scalars": np.array([r_start, ddr, FC, k, *extent]), "direct": direct, "ffbp": img.image,
+            "ffbp_axes": np.array([*img.origin, img.r0, img.dr, img.u0, img.du]),
+            "eval_points": cl, "evaluate": fast, "targets": targets, "contrib": contrib,
+            "counts": np.array([counts[k] for k in ("leaves", "merges", "leaf_pixel_pulse_products",
+                                                     "merged_pixels")], np.int64)}
+
+
+def kernels_case(ffbp):
+    rng = np.random.default_rng(77)
+    img = (rng.standard_normal((40, 36)) + 1j * rng.standard_normal((40, 36))).astype(np.complex64)
+    so = np.array([0.3, -4.0, 18.5])
+    do = np.array([0.1, 2.0, 18.2])
+    sr0, sdr, su0, sdu = 1000.0, 0.5, -0.05, 0.003
+    r0, dr, nr, u0, du, nu = 1002.0, 0.5, 30, -0.04, 0.0021, 33
+    k = -58.7
+    out = {}
+    for side in (1, -1):
+        out[f"regrid_side{side}"] = ffbp.regrid(img, so, sr0, sdr, su0, sdu, do, r0, dr, nr, u0, du, nu, k, side)
+    row = (rng.standard_normal(64) + 1j * rng.standard_normal(64)).astype(np.complex64)
+    q = np.concatenate([rng.uniform(-2, 66, 200), np.arange(-2, 66, 1.0), [0.999999, 1.0, 60.9999, 61.0, 61.0001]])
+    s1 = np.array([ffbp.sample1(row, float(v)) for v in q], np.complex128)
+    qr = rng.uniform(-2, 42, 300)
+    qu = rng.uniform(-2, 38, 300)
+    s2 = np.array([ffbp.sample2(img, float(a), float(b)) for a, b in zip(qr, qu)], np.complex128)
+    t = rng.uniform(-0.5, 1.5, 50)
+    cw = np.array([ffbp.cubic_weights(float(v)) for v in t], np.float64)
+    out.update({"image": img, "src_origin": so, "dst_origin": do,
+                "grid": np.array([sr0, sdr, su0, sdu, r0, dr, nr, u0, du, nu, k]),
+                "row": row, "q": q, "sample1": s1, "qr": qr, "qu": qu, "sample2": s2, "t": t, "cubic": cw})
+    return out
+
+
+def plans_case(gb):
+    sys.path.insert(0, str(REPO))
+    from bp_project_gb300 import scenes
+    out = {}
+    for name in ("c0", "c1", "c3"):
+        cfg = scenes.CONFIGS[name]
+        pos = scenes.trajectory(cfg)
+        extent = scenes.polar_extent(cfg, pos)
+        plan = gb.build_ffbp_plan(pos, cfg.fc, extent, side=1, leaf_size=cfg.leaf_size,
+                                  range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+        geom, idx, crop, cnt, root = flatten_plan(plan)
+        out.update({f"{name}_position": pos, f"{name}_args": np.array([cfg.fc, *extent, 1, cfg.leaf_size,
+                                                                       cfg.range_spacing, cfg.angular_oversample]),
+                    f"{name}_geom": geom, f"{name}_idx": idx, f"{name}_crop": crop, f"{name}_counts": cnt,
+                    f"{name}_root": root})
+        print(f"plan {name}: {plan.shape}, counts {plan.counts}", flush=True)
+    pos = validate_track(512)
+    plan = gb.build_ffbp_plan(pos, 1.4e9, (650, 1300, -0.5, 0.18), side=1, leaf_size=64, range_spacing=0.25,
+                              angular_oversample=3.0)
+    geom, idx, crop, cnt, root = flatten_plan(plan)
+    out.update({"validate_position": pos, "validate_args": np.array([1.4e9, 650, 1300, -0.5, 0.18, 1, 64, 0.25, 3.0]),
+                "validate_geom": geom, "validate_idx": idx, "validate_crop": crop, "validate_counts": cnt,
+                "validate_root": root})
+    # A left-looking, negative-carrier plan on the same track.
+    plan = gb.build_ffbp_plan(pos * np.array([-1, 1, 1]), -1.4e9, (650, 1300, -0.5, 0.18), side=-1, leaf_size=32,
+                              range_spacing=0.5, angular_oversample=2.0)
+    geom, idx, crop, cnt, root = flatten_plan(plan)
+    out.update({"left_position": pos * np.array([-1, 1, 1]),
+                "left_args": np.array([-1.4e9, 650, 1300, -0.5, 0.18, -1, 32, 0.5, 2.0]),
+                "left_geom": geom, "left_idx": idx, "left_crop": crop, "left_counts": cnt, "left_root": root})
+    return out
+
+
+def main():
+    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    ffbp, gb = import_reference(root)
+    np.savez_compressed(HERE / "operator_validation.npz", **operator_validation(ffbp, gb))
+    np.savez_compressed(HERE / "points.npz", **points_case(ffbp))
+    np.savez_compressed(HERE / "kernels.npz", **kernels_case(ffbp))
+    np.savez_compressed(HERE / "plans.npz", **plans_case(gb))
+
+
+if __name__ == "__main__":
+    main()
