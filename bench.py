@@ -1,0 +1,372 @@
+"""Benchmark: direct BP throughput (Gpixel*pulses/s) on the 4096-pulse / 2048^2 scene, plus FFBP img/s.
+
+Workload (one "step"): split-precision direct back-projection of 4096 pulses x
+8192 range bins (complex64, 268 MB, larger than L2) onto a 2048 x 2048 ground
+lattice at 0.5 m, fc 9.6 GHz, 150 MHz, 4 km near slant range; seeded
+synthetic scene (25 point targets over clutter scatterers).  Also reported:
+FFBP on the same scene (leaves of 16 pulses, 8 merge levels) in images/s,
+errors against the FP64 oracle, the plain FP64-phase kernel on the same
+pixels, the CPU oracle on a bounded pixel sample, and the roofline of the
+dominant kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+For N > 1 run under torch.distributed.run: every rank images its own copy of
+the scene (weak scaling, no data-path collective); the timed region is
+bracketed by barriers and the maximum over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BP Gpixel·pulses/s and FFBP img/s at stated err vs FP64; autofocus iters/s"
+UNIT = "Gpixel·pulses/s"
+WORKLOAD = "c1 direct BP: 4096 pulses x 8192 bins -> 2048x2048 ground lattice @0.5 m, 9.6 GHz, split precision"
+FP32_FLOPS_PER_PX_PULSE = 54.0      # algorithmic FP32 work per pixel-pulse (FMA = 2)
+MUFU_PER_PX_PULSE = 3.0
+CPU_SAMPLE_PIXELS = 65536           # bounded CPU-baseline sample (all 4096 pulses)
+REF_SAMPLE_PIXELS = 32768           # pixels per step of the reference arm
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ffbp", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class Clocks:
+    """Sample nvidia-smi clocks and throttle reasons while the timed region runs."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return False
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        return json.loads(path.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(scene, pixels, seed=11):
+    """FP64 oracle (C++/OpenMP restatement of the reference's Numba BP) on a bounded pixel sample."""
+    from oracle import reference as ora
+    threads = ora.set_threads(0)
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(scene.lattice.rows * scene.lattice.cols, pixels, replace=False)
+    pts = scene.lattice.take(idx)
+    t0 = time.perf_counter()
+    out = ora.backproject_points(scene.data, scene.position, pts, scene.range_start, scene.data_dr, scene.k,
+                                 scene.weight, scene.phase, c128=True)[1]
+    dt = time.perf_counter() - t0
+    return {"value": pixels * scene.config.pulses / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "seconds": dt,
+            "sample": f"{pixels} random pixels of the 2048^2 lattice x all {scene.config.pulses} pulses "
+                      f"(FP64 C++/OpenMP restatement of ffbp.backproject_points)"}, idx, out
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference's CPU BP (restated, FP64, all host threads) on a bounded sample per step."""
+    if rank != 0:
+        return
+    from bp_project_gb300 import scenes
+    from oracle import build as oracle_build
+    from oracle import reference as ora
+    oracle_build.build()
+    scene = scenes.synthesize(scenes.CONFIGS[args.config])
+    threads = ora.set_threads(0)
+    rng = np.random.default_rng(5)
+    npix = scene.lattice.rows * scene.lattice.cols
+    times = []
+    for step in range(args.warmup + args.steps):
+        pts = scene.lattice.take(rng.choice(npix, REF_SAMPLE_PIXELS, replace=False))
+        t0 = time.perf_counter()
+        ora.backproject_points(scene.data, scene.position, pts, scene.range_start, scene.data_dr, scene.k,
+                               scene.weight, scene.phase)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    per_step = statistics.mean(times)
+    value = REF_SAMPLE_PIXELS * scene.config.pulses / per_step / 1e9
+    sample = (f"{REF_SAMPLE_PIXELS} random pixels of the 2048^2 lattice x all {scene.config.pulses} pulses per step "
+              f"(FP64 C++/OpenMP restatement of ffbp.backproject_points; the reference's Numba path cannot run here)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("split precision", "FP64 CPU"), "pulses": scene.config.pulses,
+                       "samples": scene.config.samples, "image": [scene.lattice.rows, scene.lattice.cols],
+                       "sample_pixels_per_step": REF_SAMPLE_PIXELS},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    import torch.distributed as dist
+
+    from bp_project_gb300 import _native, build, core, scenes
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    cfg = scenes.CONFIGS[args.config]
+    scene = scenes.synthesize(cfg, device=str(dev))
+    lat = scene.lattice
+    npix = lat.rows * lat.cols
+    units = npix * cfg.pulses
+
+    data = torch.from_numpy(scene.data).to(dev)
+    pos = torch.from_numpy(scene.position).to(dev)
+    wt = torch.from_numpy(scene.weight).to(dev)
+    ph = torch.from_numpy(scene.phase).to(dev)
+    out = torch.empty((lat.rows, lat.cols), dtype=torch.complex64, device=dev)
+
+    def step():
+        core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                 scene.range_start, scene.data_dr, scene.k, mode="split", out=out)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    launches0 = _native.launch_count()
+    with Clocks(local) as clocks:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            step()
+            ev[i + 1].record(stream)
+        barrier()
+    launches = _native.launch_count() - launches0
+    per_launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * units * args.steps / (total_ms / 1e3) / 1e9
+    image = out.cpu().numpy()
+
+    # End to end through the public API: pinned host inputs -> device -> BP -> host image, every step.
+    host_data = torch.from_numpy(scene.data).pin_memory()
+    host_pos = torch.from_numpy(scene.position).pin_memory()
+    host_w = torch.from_numpy(scene.weight).pin_memory()
+    host_ph = torch.from_numpy(scene.phase).pin_memory()
+    host_out = torch.empty((lat.rows, lat.cols), dtype=torch.complex64).pin_memory()
+    d_data, d_pos, d_w, d_ph = (torch.empty_like(t, device=dev) for t in (host_data, host_pos, host_w, host_ph))
+
+    def e2e_step():
+        d_data.copy_(host_data, non_blocking=True)
+        d_pos.copy_(host_pos, non_blocking=True)
+        d_w.copy_(host_w, non_blocking=True)
+        d_ph.copy_(host_ph, non_blocking=True)
+        core.backproject_lattice(d_data, d_pos, d_w, d_ph, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                 scene.range_start, scene.data_dr, scene.k, mode="split", out=out)
+        host_out.copy_(out, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    h2d = sum(t.numel() * t.element_size() for t in (host_data, host_pos, host_w, host_ph))
+    d2h = host_out.numel() * host_out.element_size()
+
+    extra = {}
+    if rank == 0:
+        # Plain FP64-phase kernel (the reference's mixed policy) on the same lattice, one timed pass.
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        mixed_out = torch.empty_like(out)
+        rows_m = 256  # a 256-row band keeps the slow FP64 kernel to ~a second
+        origin_m = lat.origin
+        s0.record(stream)
+        core.backproject_lattice(data, pos, wt, ph, origin_m, lat.step_row, lat.step_col, rows_m, lat.cols,
+                                 scene.range_start, scene.data_dr, scene.k, mode="mixed", out=mixed_out[:rows_m])
+        s1.record(stream)
+        torch.cuda.synchronize()
+        mixed_rate = rows_m * lat.cols * cfg.pulses / (s0.elapsed_time(s1) / 1e3) / 1e9
+        extra["plain_fp64_phase_gpix_pulse_s"] = mixed_rate
+        extra["split_over_plain_fp64_phase"] = value / world / mixed_rate
+        band = image[:rows_m].astype(np.complex128)
+        extra["split_vs_plain_fp64_phase_err"] = float(np.linalg.norm(band - mixed_out[:rows_m].cpu().numpy())
+                                                       / np.linalg.norm(band))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import build as oracle_build
+        oracle_build.build()
+        cpu, idx, ref = cpu_baseline(scene, CPU_SAMPLE_PIXELS)
+        est = image.ravel()[idx].astype(np.complex128)
+        extra["err_vs_fp64"] = float(np.linalg.norm(est - ref) / np.linalg.norm(ref))
+        extra["err_vs_fp64_sample"] = f"{CPU_SAMPLE_PIXELS} random pixels, complex L2"
+
+    if rank == 0 and not args.no_ffbp:
+        ext = scene.extent
+        plan = build_ffbp_plan(scene.position, cfg.fc, ext, side=1, leaf_size=cfg.leaf_size,
+                               range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+        prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split", device=dev)
+        pts = torch.from_numpy(lat.points()).to(dev)
+        grid = plan.grid()
+        ground = torch.empty(npix, dtype=torch.complex64, device=dev)
+
+        def ffbp_step():
+            polar = prog.execute(data, pos, wt, ph, scene.range_start, scene.data_dr, scene.k)
+            core.evaluate_image(polar, grid, pts, scene.k, out=ground)
+            return polar
+
+        for _ in range(2):
+            ffbp_step()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nrep = max(3, args.steps // 2)
+        f0.record(stream)
+        for _ in range(nrep):
+            ffbp_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ffbp_ms = f0.elapsed_time(f1) / nrep
+        g = ground.cpu().numpy().reshape(lat.rows, lat.cols).astype(np.complex128)
+        extra.update({
+            "ffbp_img_per_s": 1e3 / ffbp_ms, "ffbp_ms": ffbp_ms,
+            "ffbp_config": f"leaf {cfg.leaf_size}, {plan.counts['leaves']} leaves, {plan.counts['merges']} merges, "
+                           f"root polar {plan.nr}x{plan.nu}, range spacing {cfg.range_spacing} m, angular oversample "
+                           f"{cfg.angular_oversample}; polar FFBP + evaluate_image onto the 2048^2 lattice",
+            "ffbp_launches": prog.launch_count + 1,
+            "ffbp_vs_direct_err": float(np.linalg.norm(g - image) / np.linalg.norm(image)),
+        })
+        prog.close()
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    peaks, peak_kind = measured_peaks()
+    clk = clocks.summary()
+    kernel_ms = statistics.mean(per_launch_ms)
+    alg_bytes = 8.0 * cfg.pulses * cfg.samples + 48.0 * cfg.pulses + 8.0 * npix  # data + pos/w/phase + image
+    achieved_gbs = alg_bytes / (kernel_ms / 1e3) / 1e9
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = units * FP32_FLOPS_PER_PX_PULSE / (kernel_ms / 1e3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (split precision: FP64 per tile-pulse)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pulses": cfg.pulses, "samples": cfg.samples,
+                   "image": [lat.rows, lat.cols], "pixel_spacing_m": cfg.pixel_spacing,
+                   "l2": "inputs larger than L2 (268 MB range data per step)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * units / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                "path": "pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), image -> host"},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                     "kernel": "split_lattice_kernel", "note": f"peak of {peak_kind}; algorithmic bytes "
+                     f"{alg_bytes / 1e6:.1f} MB per launch; the kernel is FP32/MUFU-issue bound (roofline_fp32)"},
+        "roofline_fp32": {"bound": "fp32_issue", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                          "frac": fp32_achieved / fp32_peak,
+                          "note": f"{FP32_FLOPS_PER_PX_PULSE:.0f} algorithmic FP32 flops + {MUFU_PER_PX_PULSE:.0f} "
+                                  f"MUFU per pixel-pulse; peak = {sm_count} SMs x 128 lanes x 2 x median SM clock "
+                                  f"{sm_mhz:.0f} MHz (no measured FP32 peak available)"},
+        "kernel_ms": kernel_ms,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "cpu_baseline": cpu,
+        **extra,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

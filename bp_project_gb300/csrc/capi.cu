@@ -1,0 +1,555 @@
+// extern "C" entry points of libsarbp: argument validation, dispatch to the
+// plain / split kernels, and the level-batched FFBP plan object.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sarbp {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int check_launch(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "%s launch failed: %s", what, cudaGetErrorString(e));
+    return SARBP_OK;
+}
+
+void note_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+namespace {
+
+constexpr size_t kAlign = 512;
+
+size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+bool is_finite_value(double v) { return isfinite(v) != 0; }
+
+int check_pulses(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                 const double* phase, double data_dr, double k) {
+    if (!data || !pos || !weight || !phase) return fail(SARBP_ERR_TYPE, "data, pos, weight and phase must be device pointers");
+    if (((uintptr_t)data & 7) || ((uintptr_t)pos & 7) || ((uintptr_t)weight & 7) || ((uintptr_t)phase & 7))
+        return fail(SARBP_ERR_TYPE, "arrays must be 8-byte aligned");
+    if (pulses < 1) return fail(SARBP_ERR_VALUE, "at least one pulse is required (got %d)", pulses);
+    if (samples < 1) return fail(SARBP_ERR_VALUE, "range-compressed data must have at least one sample per pulse");
+    if (!is_finite_value(data_dr) || data_dr == 0.0) return fail(SARBP_ERR_VALUE, "data_dr must be finite and non-zero");
+    if (!is_finite_value(k)) return fail(SARBP_ERR_VALUE, "k must be finite");
+    return SARBP_OK;
+}
+
+int check_mode(int mode) {
+    if (mode < SARBP_FP64 || mode > SARBP_SPLIT) return fail(SARBP_ERR_VALUE, "mode must be one of fp64, fp32, mixed, split (got %d)", mode);
+    return SARBP_OK;
+}
+
+int check_grid(const sarbp_polar_grid* g) {
+    if (!g) return fail(SARBP_ERR_TYPE, "grid must not be NULL");
+    if (g->nr <= 0 || g->nu <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    if (!is_finite_value(g->r0) || !is_finite_value(g->dr) || !is_finite_value(g->u0) || !is_finite_value(g->du) || !is_finite_value(g->origin[0]) ||
+        !is_finite_value(g->origin[1]) || !is_finite_value(g->origin[2]))
+        return fail(SARBP_ERR_VALUE, "grid geometry must be finite");
+    if (g->side != 1 && g->side != -1) return fail(SARBP_ERR_VALUE, "side must be +1 or -1");
+    return SARBP_OK;
+}
+
+PolarDesc desc_of(const sarbp_polar_grid& g) {
+    PolarDesc d{};
+    d.ox = g.origin[0];
+    d.oy = g.origin[1];
+    d.oz = g.origin[2];
+    d.r0 = g.r0;
+    d.dr = g.dr;
+    d.u0 = g.u0;
+    d.du = g.du;
+    d.nr = g.nr;
+    d.nu = g.nu;
+    d.side = g.side;
+    d.left = d.right = -1;
+    d.win_r0 = 0;
+    d.win_u0 = 0;
+    d.win_nr = g.nr;
+    d.win_nu = g.nu;
+    d.out_offset = 0;
+    d.out_stride = g.nu;
+    d.tile_lc = 5;
+    return d;
+}
+
+PulseInputs inputs_of(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                      const double* phase, double range_start, double data_dr, double k) {
+    PulseInputs in;
+    in.data = reinterpret_cast<const float2*>(data);
+    in.pulses = pulses;
+    in.samples = samples;
+    in.pos = pos;
+    in.weight = weight;
+    in.phase = phase;
+    in.range_start = range_start;
+    in.data_dr = data_dr;
+    in.k = k;
+    return in;
+}
+
+double lattice_radius(const sarbp_lattice& lat, int lc) {
+    const double hr = (double)((kSplitTilePixels >> lc) >> 1), hc = (double)((1 << lc) >> 1);
+    double s = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        const double b = hr * fabs(lat.step_row[c]) + hc * fabs(lat.step_col[c]);
+        s += b * b;
+    }
+    return sqrt(s) * 1.0001 + 1e-6;
+}
+
+// Envelope assumed for point tiles: tiles wider than this run through the FP64 fallback.
+constexpr double kPointRadius = 24.0;
+
+}  // namespace
+}  // namespace sarbp
+
+using namespace sarbp;
+
+// ---- FFBP plan object -------------------------------------------------------------------
+struct sarbp_ffbp_plan {
+    int mode = SARBP_SPLIT;
+    int n_nodes = 0;
+    std::vector<PolarDesc> nodes;
+    std::vector<int> height;
+    int max_height = 0;
+    // Split: tile items; plain: 256-pixel blocks.  Stage h occupies [stage_begin[h], +stage_count[h]).
+    std::vector<TileItem> items;
+    std::vector<int2> blocks;
+    std::vector<int> stage_begin, stage_count;
+    int leaf_chunk = 1, leaf_wb = 4;
+    size_t node_bytes = 0, work_bytes = 0, arena_offset = 0, arena_bytes = 0, total_bytes = 0;
+    void* bound = nullptr;
+    size_t bound_bytes = 0;
+    int launches = 0;
+};
+
+extern "C" {
+
+const char* sarbp_version(void) { return "libsarbp 0.1.0 (sm_103a)"; }
+int sarbp_abi_version(void) { return SARBP_ABI_VERSION; }
+
+const char* sarbp_status_string(int status) {
+    switch (status) {
+        case SARBP_OK: return "ok";
+        case SARBP_ERR_VALUE: return "invalid value";
+        case SARBP_ERR_TYPE: return "invalid pointer or type";
+        case SARBP_ERR_WORKSPACE: return "workspace missing or too small";
+        case SARBP_ERR_CUDA: return "CUDA error";
+        case SARBP_ERR_PLAN: return "FFBP plan error";
+        case SARBP_ERR_ENVELOPE: return "outside the split-precision envelope";
+        default: return "unknown status";
+    }
+}
+
+const char* sarbp_last_error(void) { return g_last_error.c_str(); }
+uint64_t sarbp_launch_count(void) { return g_launches.load(); }
+
+// ---- direct BP ---------------------------------------------------------------------------
+size_t sarbp_direct_polar_workspace(int mode, const sarbp_polar_grid* grid, int pulses, int pulse_split) {
+    (void)mode;
+    (void)pulses;
+    if (!grid || pulse_split <= 1) return 0;
+    return (size_t)pulse_split * (size_t)grid->nr * (size_t)grid->nu * sizeof(float2);
+}
+
+int sarbp_direct_polar(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                       const double* phase, const sarbp_polar_grid* grid, double range_start, double data_dr,
+                       double k, int mode, int chunk_pulses, int pulse_split, float* out, void* workspace,
+                       size_t workspace_bytes, void* stream) {
+    if (int st = check_mode(mode)) return st;
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (int st = check_grid(grid)) return st;
+    if (!out) return fail(SARBP_ERR_TYPE, "out must not be NULL");
+    if (chunk_pulses <= 0) return fail(SARBP_ERR_VALUE, "chunk_pulses must be positive");
+    if (pulse_split < 1 || pulse_split > pulses) return fail(SARBP_ERR_VALUE, "pulse_split must be in [1, pulses]");
+    const size_t need = sarbp_direct_polar_workspace(mode, grid, pulses, pulse_split);
+    if (need && (!workspace || workspace_bytes < need))
+        return fail(SARBP_ERR_WORKSPACE, "direct_polar needs %zu workspace bytes", need);
+    cudaStream_t s = (cudaStream_t)stream;
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    PolarDesc g = desc_of(*grid);
+    g.a = 0;
+    g.b = pulses;
+    float2* dst = reinterpret_cast<float2*>(out);
+    float2* parts = pulse_split > 1 ? reinterpret_cast<float2*>(workspace) : dst;
+    const long long npix = (long long)grid->nr * grid->nu;
+    int st;
+    if (mode == SARBP_SPLIT) {
+        double radius = 0.0;
+        g.tile_lc = split_polar_tile_lc(g, &radius);
+        const int wb = split_window_bins(radius, data_dr);
+        const int ch = split_chunk_for(wb, chunk_pulses);
+        st = launch_split_polar(in, g, pulse_split, ch, wb, parts, g.nu, npix, s);
+    } else {
+        st = SARBP_OK;
+        for (int part = 0; part < pulse_split && st == SARBP_OK; ++part) {
+            const int p0 = (int)((long long)pulses * part / pulse_split);
+            const int p1 = (int)((long long)pulses * (part + 1) / pulse_split);
+            st = launch_plain_polar(mode, in, g, p0, p1, chunk_pulses, parts + part * npix, g.nu, s);
+        }
+    }
+    if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(parts, pulse_split, npix, npix, dst, s);
+    return st;
+}
+
+size_t sarbp_backproject_points_workspace(int mode, int npts, int pulse_split) {
+    (void)mode;
+    if (pulse_split <= 1 || npts <= 0) return 0;
+    return (size_t)pulse_split * (size_t)npts * sizeof(float2);
+}
+
+int sarbp_backproject_points(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                             const double* phase, const double* xyz, int npts, double range_start, double data_dr,
+                             double k, int mode, int pulse_split, float* out, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+    if (int st = check_mode(mode)) return st;
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (!xyz || !out) return fail(SARBP_ERR_TYPE, "xyz and out must not be NULL");
+    if (npts <= 0) return fail(SARBP_ERR_VALUE, "at least one point is required");
+    if (pulse_split < 1 || pulse_split > pulses) return fail(SARBP_ERR_VALUE, "pulse_split must be in [1, pulses]");
+    if (mode != SARBP_SPLIT && pulse_split != 1) return fail(SARBP_ERR_VALUE, "pulse_split applies to split mode only");
+    const size_t need = sarbp_backproject_points_workspace(mode, npts, pulse_split);
+    if (need && (!workspace || workspace_bytes < need))
+        return fail(SARBP_ERR_WORKSPACE, "backproject_points needs %zu workspace bytes", need);
+    cudaStream_t s = (cudaStream_t)stream;
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    float2* dst = reinterpret_cast<float2*>(out);
+    if (mode != SARBP_SPLIT) return launch_plain_points(mode, in, xyz, npts, 0, dst, s);
+    float2* parts = pulse_split > 1 ? reinterpret_cast<float2*>(workspace) : dst;
+    const int wb = split_window_bins(kPointRadius, data_dr);
+    const int ch = split_chunk_for(wb, 64);
+    int st = launch_split_points(in, xyz, npts, pulse_split, ch, wb, parts, npts, s);
+    if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(parts, pulse_split, npts, npts, dst, s);
+    return st;
+}
+
+size_t sarbp_backproject_lattice_workspace(int mode, const sarbp_lattice* lattice, int pulse_split) {
+    (void)mode;
+    if (!lattice || pulse_split <= 1) return 0;
+    return (size_t)pulse_split * (size_t)lattice->rows * (size_t)lattice->cols * sizeof(float2);
+}
+
+int sarbp_backproject_lattice(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                              const double* phase, const sarbp_lattice* lattice, double range_start,
+                              double data_dr, double k, int mode, int pulse_split, float* out, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+    if (int st = check_mode(mode)) return st;
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (!lattice || !out) return fail(SARBP_ERR_TYPE, "lattice and out must not be NULL");
+    if (lattice->rows <= 0 || lattice->cols <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    for (int c = 0; c < 3; ++c)
+        if (!is_finite_value(lattice->origin[c]) || !is_finite_value(lattice->step_row[c]) || !is_finite_value(lattice->step_col[c]))
+            return fail(SARBP_ERR_VALUE, "lattice geometry must be finite");
+    if (pulse_split < 1 || pulse_split > pulses) return fail(SARBP_ERR_VALUE, "pulse_split must be in [1, pulses]");
+    if (mode != SARBP_SPLIT && pulse_split != 1) return fail(SARBP_ERR_VALUE, "pulse_split applies to split mode only");
+    const size_t need = sarbp_backproject_lattice_workspace(mode, lattice, pulse_split);
+    if (need && (!workspace || workspace_bytes < need))
+        return fail(SARBP_ERR_WORKSPACE, "backproject_lattice needs %zu workspace bytes", need);
+    cudaStream_t s = (cudaStream_t)stream;
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    float2* dst = reinterpret_cast<float2*>(out);
+    if (mode != SARBP_SPLIT) return launch_plain_lattice(mode, in, *lattice, 0, dst, s);
+    const long long npix = (long long)lattice->rows * lattice->cols;
+    float2* parts = pulse_split > 1 ? reinterpret_cast<float2*>(workspace) : dst;
+    const int wb = split_window_bins(lattice_radius(*lattice, 5), data_dr);
+    const int ch = split_chunk_for(wb, 64);
+    int st = launch_split_lattice(in, *lattice, pulse_split, ch, wb, parts, npix, s);
+    if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(parts, pulse_split, npix, npix, dst, s);
+    return st;
+}
+
+// ---- FFBP building blocks ---------------------------------------------------------------
+int sarbp_regrid(const float* image, const sarbp_polar_grid* src, const sarbp_polar_grid* dst, double k, int mode,
+                 float* out, void* stream) {
+    if (int st = check_mode(mode)) return st;
+    if (!image || !out) return fail(SARBP_ERR_TYPE, "image and out must not be NULL");
+    if (int st = check_grid(src)) return st;
+    if (int st = check_grid(dst)) return st;
+    if (!is_finite_value(k)) return fail(SARBP_ERR_VALUE, "k must be finite");
+    const int m = mode == SARBP_SPLIT ? SARBP_MIXED : mode;
+    return launch_plain_regrid(m, reinterpret_cast<const float2*>(image), desc_of(*src), desc_of(*dst), k,
+                               reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+int sarbp_merge_regrid(const float* left, const sarbp_polar_grid* left_grid, const float* right,
+                       const sarbp_polar_grid* right_grid, const sarbp_polar_grid* dst, double k, int mode, float* out,
+                       void* stream) {
+    if (int st = check_mode(mode)) return st;
+    if (!left || !right || !out) return fail(SARBP_ERR_TYPE, "images and out must not be NULL");
+    if (int st = check_grid(left_grid)) return st;
+    if (int st = check_grid(right_grid)) return st;
+    if (int st = check_grid(dst)) return st;
+    if (!is_finite_value(k)) return fail(SARBP_ERR_VALUE, "k must be finite");
+    const int m = mode == SARBP_SPLIT ? SARBP_MIXED : mode;
+    return launch_plain_merge(m, reinterpret_cast<const float2*>(left), desc_of(*left_grid),
+                              reinterpret_cast<const float2*>(right), desc_of(*right_grid), desc_of(*dst), k,
+                              reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+int sarbp_add_inplace(float* left, const float* right, int64_t n, void* stream) {
+    if (!left || !right) return fail(SARBP_ERR_TYPE, "left and right must not be NULL");
+    if (n <= 0) return fail(SARBP_ERR_VALUE, "n must be positive");
+    return launch_add(reinterpret_cast<float2*>(left), reinterpret_cast<const float2*>(right), n, (cudaStream_t)stream);
+}
+
+int sarbp_cast_c128_to_c64(const double* in, float* out, int64_t n, void* stream) {
+    if (!in || !out) return fail(SARBP_ERR_TYPE, "in and out must not be NULL");
+    if (n <= 0) return fail(SARBP_ERR_VALUE, "n must be positive");
+    return launch_cast(reinterpret_cast<const double2*>(in), reinterpret_cast<float2*>(out), n, (cudaStream_t)stream);
+}
+
+int sarbp_crop(const float* in, int src_nu, int r_begin, int u_begin, int nr, int nu, float* out, void* stream) {
+    if (!in || !out) return fail(SARBP_ERR_TYPE, "in and out must not be NULL");
+    if (nr <= 0 || nu <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    if (r_begin < 0 || u_begin < 0 || u_begin + nu > src_nu)
+        return fail(SARBP_ERR_VALUE, "crop window outside the source image");
+    return launch_crop(reinterpret_cast<const float2*>(in), src_nu, r_begin, u_begin, nr, nu,
+                       reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+// ---- FFBP plan -------------------------------------------------------------------------
+int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r0, int crop_u0, int crop_nr,
+                           int crop_nu, int mode, sarbp_ffbp_plan** plan_out) {
+    if (!plan_out) return fail(SARBP_ERR_TYPE, "plan pointer must not be NULL");
+    *plan_out = nullptr;
+    if (int st = check_mode(mode)) return st;
+    if (!nodes || n_nodes < 1) return fail(SARBP_ERR_VALUE, "an FFBP plan needs at least one node");
+    const sarbp_ffbp_node& root = nodes[0];
+    if (crop_nr <= 0 || crop_nu <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    if (crop_r0 < 0 || crop_u0 < 0 || crop_r0 + crop_nr > root.nr || crop_u0 + crop_nu > root.nu)
+        return fail(SARBP_ERR_VALUE, "crop window outside the root grid");
+    auto* p = new sarbp_ffbp_plan();
+    p->mode = mode;
+    p->n_nodes = n_nodes;
+    p->nodes.resize(n_nodes);
+    p->height.assign(n_nodes, -1);
+    for (int i = 0; i < n_nodes; ++i) {
+        const sarbp_ffbp_node& n = nodes[i];
+        sarbp_polar_grid g{};
+        for (int c = 0; c < 3; ++c) g.origin[c] = n.origin[c];
+        g.r0 = n.r0;
+        g.dr = n.dr;
+        g.u0 = n.u0;
+        g.du = n.du;
+        g.nr = n.nr;
+        g.nu = n.nu;
+        g.side = n.side;
+        if (int st = check_grid(&g)) {
+            delete p;
+            return fail(st, "node %d: %s", i, g_last_error.c_str());
+        }
+        const bool leaf = n.left < 0 && n.right < 0;
+        if (!leaf && (n.left <= i || n.right <= i || n.left >= n_nodes || n.right >= n_nodes)) {
+            delete p;
+            return fail(SARBP_ERR_PLAN, "node %d: children must follow their parent in pre-order", i);
+        }
+        if (leaf && (n.a < 0 || n.b <= n.a)) {
+            delete p;
+            return fail(SARBP_ERR_PLAN, "leaf %d: invalid pulse range [%d, %d)", i, n.a, n.b);
+        }
+        PolarDesc d = desc_of(g);
+        d.a = n.a;
+        d.b = n.b;
+        d.left = leaf ? -1 : n.left;
+        d.right = leaf ? -1 : n.right;
+        p->nodes[i] = d;
+    }
+    // Heights (children follow parents, so a reverse sweep sees children first).
+    for (int i = n_nodes - 1; i >= 0; --i) {
+        const PolarDesc& d = p->nodes[i];
+        p->height[i] = d.left < 0 ? 0 : 1 + std::max(p->height[d.left], p->height[d.right]);
+    }
+    p->max_height = p->height[0];
+    // Windows, arena offsets, tile shapes.
+    size_t arena = 0;
+    double leaf_radius = 0.0;
+    int leaf_pulses = 1;
+    for (int i = 0; i < n_nodes; ++i) {
+        PolarDesc& d = p->nodes[i];
+        if (i == 0) {
+            d.win_r0 = crop_r0;
+            d.win_u0 = crop_u0;
+            d.win_nr = crop_nr;
+            d.win_nu = crop_nu;
+            d.out_offset = 0;
+            d.out_stride = crop_nu;
+        } else {
+            d.out_offset = (long long)(arena / sizeof(float2));
+            d.out_stride = d.nu;
+            arena += align_up((size_t)d.nr * d.nu * sizeof(float2));
+        }
+        double radius = 0.0;
+        d.tile_lc = split_polar_tile_lc(d, &radius);
+        if (d.left < 0) {
+            leaf_radius = std::max(leaf_radius, radius);
+            leaf_pulses = std::max(leaf_pulses, d.b - d.a);
+        }
+    }
+    p->leaf_wb = std::max(4, split_window_bins(leaf_radius, 1.0));  // rescaled at execute for data_dr
+    // Work lists per stage.
+    p->stage_begin.assign(p->max_height + 1, 0);
+    p->stage_count.assign(p->max_height + 1, 0);
+    for (int h = 0; h <= p->max_height; ++h) {
+        p->stage_begin[h] = mode == SARBP_SPLIT ? (int)p->items.size() : (int)p->blocks.size();
+        for (int i = 0; i < n_nodes; ++i) {
+            if (p->height[i] != h) continue;
+            const PolarDesc& d = p->nodes[i];
+            if (mode == SARBP_SPLIT) {
+                const int cols_t = 1 << d.tile_lc, rows_t = kSplitTilePixels >> d.tile_lc;
+                for (int r = 0; r < d.win_nr; r += rows_t)
+                    for (int u = 0; u < d.win_nu; u += cols_t) p->items.push_back(TileItem{i, r, u, 0});
+            } else {
+                const long long npix = (long long)d.win_nr * d.win_nu;
+                for (long long s = 0; s < npix; s += 256) p->blocks.push_back(make_int2(i, (int)s));
+            }
+        }
+        p->stage_count[h] = (mode == SARBP_SPLIT ? (int)p->items.size() : (int)p->blocks.size()) - p->stage_begin[h];
+    }
+    if ((mode == SARBP_SPLIT ? p->items.size() : p->blocks.size()) > (size_t)INT32_MAX) {
+        delete p;
+        return fail(SARBP_ERR_PLAN, "plan too large");
+    }
+    p->leaf_chunk = leaf_pulses;
+    p->node_bytes = align_up(sizeof(PolarDesc) * n_nodes);
+    p->work_bytes = align_up(mode == SARBP_SPLIT ? sizeof(TileItem) * p->items.size() : sizeof(int2) * p->blocks.size());
+    p->arena_offset = p->node_bytes + p->work_bytes;
+    p->arena_bytes = arena;
+    p->total_bytes = p->arena_offset + arena;
+    p->launches = p->max_height + 1;
+    *plan_out = p;
+    return SARBP_OK;
+}
+
+void sarbp_ffbp_plan_destroy(sarbp_ffbp_plan* plan) { delete plan; }
+
+size_t sarbp_ffbp_workspace_bytes(const sarbp_ffbp_plan* plan) { return plan ? plan->total_bytes : 0; }
+
+int sarbp_ffbp_launch_count(const sarbp_ffbp_plan* plan) { return plan ? plan->launches : 0; }
+
+int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (!workspace || workspace_bytes < plan->total_bytes)
+        return fail(SARBP_ERR_WORKSPACE, "FFBP plan needs %zu workspace bytes", plan->total_bytes);
+    if ((uintptr_t)workspace % 256) return fail(SARBP_ERR_TYPE, "workspace must be 256-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    char* base = reinterpret_cast<char*>(workspace);
+    cudaError_t e = cudaMemcpyAsync(base, plan->nodes.data(), sizeof(PolarDesc) * plan->n_nodes,
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        if (plan->mode == SARBP_SPLIT)
+            e = cudaMemcpyAsync(base + plan->node_bytes, plan->items.data(), sizeof(TileItem) * plan->items.size(),
+                                cudaMemcpyHostToDevice, s);
+        else
+            e = cudaMemcpyAsync(base + plan->node_bytes, plan->blocks.data(), sizeof(int2) * plan->blocks.size(),
+                                cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "FFBP bind: %s", cudaGetErrorString(e));
+    plan->bound = workspace;
+    plan->bound_bytes = workspace_bytes;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulses, int samples, const double* pos,
+                       const double* weight, const double* phase, double range_start, double data_dr, double k,
+                       float* out, void* stream) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (!plan->bound) return fail(SARBP_ERR_PLAN, "sarbp_ffbp_bind must succeed before execute");
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (!out) return fail(SARBP_ERR_TYPE, "out must not be NULL");
+    for (int i = 0; i < plan->n_nodes; ++i)
+        if (plan->nodes[i].left < 0 && plan->nodes[i].b > pulses)
+            return fail(SARBP_ERR_PLAN, "leaf %d uses pulses beyond the %d supplied", i, pulses);
+    cudaStream_t s = (cudaStream_t)stream;
+    char* base = reinterpret_cast<char*>(plan->bound);
+    const PolarDesc* nodes = reinterpret_cast<const PolarDesc*>(base);
+    float2* arena = reinterpret_cast<float2*>(base + plan->arena_offset);
+    float2* root_out = reinterpret_cast<float2*>(out);
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    int st = SARBP_OK;
+    if (plan->mode == SARBP_SPLIT) {
+        const TileItem* items = reinterpret_cast<const TileItem*>(base + plan->node_bytes);
+        // leaf_wb was sized for unit sample spacing; rescale to this data_dr.
+        double rad = 0.0;
+        for (int i = 0; i < plan->n_nodes; ++i)
+            if (plan->nodes[i].left < 0) {
+                double r = 0.0;
+                split_polar_tile_lc(plan->nodes[i], &r);
+                rad = std::max(rad, r);
+            }
+        const int wb = split_window_bins(rad, data_dr);
+        const int ch = split_chunk_for(wb, plan->leaf_chunk);
+        st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb, arena,
+                                      root_out, 0, s);
+        for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h)
+            st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], arena,
+                                          root_out, 0, s);
+    } else {
+        const int2* blocks = reinterpret_cast<const int2*>(base + plan->node_bytes);
+        st = launch_plain_ffbp_leaves(plan->mode, in, nodes, blocks + plan->stage_begin[0], plan->stage_count[0],
+                                      arena, s);
+        for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h)
+            st = launch_plain_ffbp_merges(plan->mode, k, nodes, blocks + plan->stage_begin[h], plan->stage_count[h],
+                                          arena, root_out, 0, s);
+    }
+    return st;
+}
+
+// ---- polar -> Cartesian, autofocus helpers, LUT probe ---------------------------------------
+int sarbp_evaluate_image(const float* image, const sarbp_polar_grid* grid, const double* xyz, int npts, double k,
+                         float* out, void* stream) {
+    if (!image || !xyz || !out) return fail(SARBP_ERR_TYPE, "image, xyz and out must not be NULL");
+    if (int st = check_grid(grid)) return st;
+    if (npts <= 0) return fail(SARBP_ERR_VALUE, "at least one point is required");
+    if (!is_finite_value(k)) return fail(SARBP_ERR_VALUE, "k must be finite");
+    return launch_evaluate(reinterpret_cast<const float2*>(image), desc_of(*grid), xyz, npts, k,
+                           reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+int sarbp_target_contributions(const float* data, int pulses, int samples, const double* pos, const double* xyz,
+                               int npts, double range_start, double data_dr, double k, float* out, void* stream) {
+    if (!data || !pos || !xyz || !out) return fail(SARBP_ERR_TYPE, "data, pos, xyz and out must not be NULL");
+    if (pulses < 1 || samples < 1 || npts < 1) return fail(SARBP_ERR_VALUE, "pulses, samples and npts must be positive");
+    if (!is_finite_value(data_dr) || data_dr == 0.0 || !is_finite_value(k)) return fail(SARBP_ERR_VALUE, "data_dr and k must be finite, data_dr non-zero");
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, nullptr, nullptr, range_start, data_dr, k);
+    return launch_target_contrib(in, xyz, npts, reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+int sarbp_fill_range_phase_lut(int samples, double range_start, double data_dr, double k, float* lut, void* stream) {
+    if (!lut) return fail(SARBP_ERR_TYPE, "lut must not be NULL");
+    if (samples < 1) return fail(SARBP_ERR_VALUE, "samples must be positive");
+    return launch_fill_lut(samples, range_start, data_dr, k, reinterpret_cast<float2*>(lut), (cudaStream_t)stream);
+}
+
+int sarbp_direct_polar_lut(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                           const double* phase, const sarbp_polar_grid* grid, double range_start, double data_dr,
+                           double k, const float* lut, float* out, void* stream) {
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (int st = check_grid(grid)) return st;
+    if (!lut || !out) return fail(SARBP_ERR_TYPE, "lut and out must not be NULL");
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    return launch_plain_polar_lut(in, desc_of(*grid), reinterpret_cast<const float2*>(lut),
+                                  reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+}  // extern "C"

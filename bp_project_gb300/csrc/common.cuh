@@ -1,0 +1,164 @@
+// Shared device helpers and internal launcher declarations for libsarbp.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sarbp.h"
+
+namespace sarbp {
+
+// x + kMagic - kMagic rounds |x| < 2^22 to the nearest integer in FP32, and
+// the bit pattern of (x + kMagic) is kMagicBits + round(x).
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+constexpr double kInvTwoPi = 0.159154943091895335768883763372514362;
+constexpr float kTwoPiF = 6.28318530717958647692f;
+
+// ---- host-side bookkeeping (capi.cu) -----------------------------------------
+int fail(int status, const char* fmt, ...);
+int check_launch(const char* what);
+void note_launches(int n);
+
+inline int grid_blocks(int64_t count, int block) { return (int)((count + block - 1) / block); }
+
+// ---- device helpers ------------------------------------------------------------
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float round_magic(float x) { return (x + kMagic) - kMagic; }
+
+// Four-point Lagrange weights at taps i-1..i+2 for fraction t, written as in
+// the reference (fast_bp/gpu/kernels.cu:8-20, ffbp.py:17-21).
+template <class T>
+__device__ __forceinline__ void lagrange_ref(T t, T w[4]) {
+    w[0] = -t * (t - T(1)) * (t - T(2)) / T(6);
+    w[1] = (t + T(1)) * (t - T(1)) * (t - T(2)) / T(2);
+    w[2] = -(t + T(1)) * t * (t - T(2)) / T(2);
+    w[3] = (t + T(1)) * t * (t - T(1)) / T(6);
+}
+
+// Lagrange weights in the centred variable s = t - 1/2 in [-1/2, 1/2]; the
+// same cubic as lagrange_ref, with nine FP32 operations and no division.
+__device__ __forceinline__ void lagrange_centred(float s, float w[4]) {
+    const float a = fmaf(s, s, -0.25f);     // s^2 - 1/4
+    const float a6 = a * (1.0f / 6.0f);
+    const float b2 = fmaf(a, 0.5f, -1.0f);  // (s^2 - 9/4) / 2
+    const float c1 = 1.5f * a6;
+    const float c2 = 0.5f * b2;
+    w[0] = fmaf(-a6, s, c1);
+    w[3] = fmaf(a6, s, c1);
+    w[1] = fmaf(b2, s, -c2);
+    w[2] = fmaf(-b2, s, -c2);
+}
+
+// Horner coefficients of the interpolating cubic through taps x0..x3 (at
+// t = -1, 0, 1, 2) in s = t - 1/2: v(s) = ((C3 s + C2) s + C1) s + C0.
+__device__ __forceinline__ void cubic_coefficients(float2 x0, float2 x1, float2 x2, float2 x3, float a,
+                                                   float4& c01, float4& c23) {
+    const float s03r = x0.x + x3.x, s03i = x0.y + x3.y;
+    const float s12r = x1.x + x2.x, s12i = x1.y + x2.y;
+    const float d30r = x3.x - x0.x, d30i = x3.y - x0.y;
+    const float d21r = x2.x - x1.x, d21i = x2.y - x1.y;
+    c01.x = a * fmaf(9.0f / 16.0f, s12r, -(1.0f / 16.0f) * s03r);
+    c01.y = a * fmaf(9.0f / 16.0f, s12i, -(1.0f / 16.0f) * s03i);
+    c01.z = a * fmaf(9.0f / 8.0f, d21r, -(1.0f / 24.0f) * d30r);
+    c01.w = a * fmaf(9.0f / 8.0f, d21i, -(1.0f / 24.0f) * d30i);
+    c23.x = a * 0.25f * (s03r - s12r);
+    c23.y = a * 0.25f * (s03i - s12i);
+    c23.z = a * fmaf(1.0f / 6.0f, d30r, -0.5f * d21r);
+    c23.w = a * fmaf(1.0f / 6.0f, d30i, -0.5f * d21i);
+}
+
+// Split a FP64 value into a multiple of 2^e (exact in FP32 when |v| < 2^(e+24))
+// and a FP32 remainder.
+__device__ __forceinline__ void quantize(double v, double scale, double inv_scale, float& hi, float& lo) {
+    const double h = rint(v * inv_scale) * scale;
+    hi = (float)h;
+    lo = (float)(v - h);
+}
+
+// ---- descriptors shared by the split and plain FFBP paths ----------------------
+struct PolarDesc {
+    double ox, oy, oz;
+    double r0, dr, u0, du;
+    int nr, nu, side;
+    int a, b;        // pulse range for leaves / direct jobs
+    int left, right; // child nodes (-1 for leaves)
+    int win_r0, win_u0, win_nr, win_nu;  // computed window of the grid
+    long long out_offset;                // element offset of the output image in the image arena
+    long long out_stride;                // row stride (elements) of the output image
+    int tile_lc;                         // split kernels: log2 of tile columns (2..5); tile rows = 1024 >> tile_lc
+    int pad;
+};
+
+struct TileItem {
+    int node;
+    int tile_r;  // first window row of the tile
+    int tile_u;  // first window col of the tile
+    int pad;
+};
+
+// ---- launchers (defined in plain.cu / split.cu) ------------------------------
+struct PulseInputs {
+    const float2* data;
+    int pulses, samples;
+    const double* pos;
+    const double* weight;
+    const double* phase;
+    double range_start, data_dr, k;
+};
+
+// Plain (reference-arithmetic) kernels.
+int launch_plain_polar(int mode, const PulseInputs& in, const PolarDesc& g, int pulse_begin, int pulse_end,
+                       int chunk, float2* out, long long out_stride, cudaStream_t s);
+int launch_plain_points(int mode, const PulseInputs& in, const double* xyz, int npts, int chunk, float2* out,
+                        cudaStream_t s);
+int launch_plain_lattice(int mode, const PulseInputs& in, const sarbp_lattice& lat, int chunk, float2* out,
+                         cudaStream_t s);
+int launch_plain_regrid(int mode, const float2* img, const PolarDesc& src, const PolarDesc& dst, double k,
+                        float2* out, cudaStream_t s);
+int launch_plain_merge(int mode, const float2* left, const PolarDesc& lg, const float2* right,
+                       const PolarDesc& rg, const PolarDesc& dst, double k, float2* out, cudaStream_t s);
+int launch_plain_ffbp_leaves(int mode, const PulseInputs& in, const PolarDesc* nodes, const int2* blocks,
+                             int nblocks, float2* arena, cudaStream_t s);
+int launch_plain_ffbp_merges(int mode, double k, const PolarDesc* nodes, const int2* blocks, int nblocks,
+                             float2* arena, float2* root_out, int root, cudaStream_t s);
+int launch_evaluate(const float2* img, const PolarDesc& g, const double* xyz, int npts, double k, float2* out,
+                    cudaStream_t s);
+int launch_target_contrib(const PulseInputs& in, const double* xyz, int npts, float2* out, cudaStream_t s);
+int launch_fill_lut(int samples, double range_start, double data_dr, double k, float2* lut, cudaStream_t s);
+int launch_plain_polar_lut(const PulseInputs& in, const PolarDesc& g, const float2* lut, float2* out,
+                           cudaStream_t s);
+int launch_add(float2* left, const float2* right, int64_t n, cudaStream_t s);
+int launch_cast(const double2* in, float2* out, int64_t n, cudaStream_t s);
+int launch_crop(const float2* in, int src_nu, int r_begin, int u_begin, int nr, int nu, float2* out,
+                cudaStream_t s);
+int launch_sum_parts(const float2* parts, int nparts, long long part_stride, long long n, float2* out,
+                     cudaStream_t s);
+
+// Split-precision kernels.
+constexpr int kSplitThreads = 256;
+constexpr int kSplitTilePixels = 1024;  // 256 threads x 4 pixels
+// Bins each pulse window needs for tiles of at most `radius` metres (pixel offset from the tile centre).
+int split_window_bins(double radius, double data_dr);
+// Pulses per shared-memory chunk that fit `window_bins` within the shared-memory budget.
+int split_chunk_for(int window_bins, int requested);
+// Tile column exponent (2..5) that makes a polar tile of grid g closest to square in metres,
+// and the largest pixel offset from the tile centre (metres) over the grid for that shape.
+int split_polar_tile_lc(const PolarDesc& g, double* radius);
+int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_split, int chunk, int window_bins,
+                       float2* out, long long out_stride, long long split_stride, cudaStream_t s);
+int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk,
+                         int window_bins, float2* out, long long split_stride, cudaStream_t s);
+int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
+                        int window_bins, float2* out, long long split_stride, cudaStream_t s);
+int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
+                             int chunk, int window_bins, float2* arena, float2* root_out, int root, cudaStream_t s);
+int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems, float2* arena,
+                             float2* root_out, int root, cudaStream_t s);
+
+}  // namespace sarbp

@@ -1,0 +1,866 @@
+// Split-precision back-projection kernels (the fast path).
+//
+// Work unit: one CTA = one tile of 1024 output pixels (256 threads x 4 pixels),
+// looping over its pulses in shared-memory chunks.  Precision plan (per pixel p,
+// pulse n, tile centre c, all FP64 work is per tile or per (tile, pulse)):
+//
+//   d(p,n) = R + L + eps,    R = |c - pos_n| (FP64, per tile-pulse)
+//                            L = u . delta_p  (u = (c - pos_n)/R, delta_p = p - c)
+//                            eps = |delta_p x u|^2 / (R + L + d)   (<= ~1 cm, FP32)
+//   phase turns = frac(K R + phase_n / 2pi)            FP64 -> FP32, per tile-pulse
+//               + frac(K u . delta_p)                  exact: W_hi . delta_hi
+//               + W_hi . delta_lo + W_lo . delta_p     FP32, tiny terms
+//               + K eps - K r_p (polar demodulation, per pixel)
+//
+// with K = k / 2pi, W = K u.  W_hi is a multiple of 2^eW with <= 10 significant
+// bits and delta_hi a multiple of 2^ed with <= 12 (2-D) / 11 (3-D) bits, so each
+// product and their sum are exact in FP32 and the large linear phase term is
+// reduced modulo one turn without rounding.  The reduced phase feeds the
+// hardware sin/cos (MUFU) on [-pi, pi).
+//
+// Range interpolation: for each (tile, pulse) the chunk stages the range bins
+// the tile can touch as Horner coefficients of the reference's four-point
+// Lagrange cubic (weight folded in), 32 bytes per bin; a pixel-pulse is then
+// two 16-byte shared loads and six FMAs.  Bins whose taps leave the row are
+// stored as zero, which reproduces the reference's support rule
+// (fast_bp/ffbp.py:27).  A tile whose window would not fit the staged bins
+// runs a chunk through an FP64 per-sample fallback instead.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace sarbp {
+namespace {
+
+constexpr int kThreads = kSplitThreads;
+constexpr int kPX = 4;
+constexpr int kMaxRows = kSplitTilePixels >> 2;  // tile_lc >= 2
+constexpr int kMaxCols = 32;                     // tile_lc <= 5
+constexpr int kMaxChunk = 64;
+constexpr int kWindowBudget = 96 * 1024;
+
+enum { kPolar = 0, kLattice = 1, kPoints = 2 };
+
+struct Rec {
+    float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y
+    float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2
+    float4 c;  // Phi, window bias bits, W_hi.z, W_lo.z
+    float4 d;  // u.z
+};
+
+struct Pix {
+    float dx, dy, dz;
+    float dxh, dyh, dzh;
+    float dxl, dyl, dzl;
+    float d2, psi;
+    float ar, ai;
+};
+
+struct TileShared {
+    double cx, cy, cz;
+    double rho;
+    double scale_d, inv_scale_d;
+    double sum[4];
+    float red[8][8];
+    int base[kMaxChunk];
+    float wt[kMaxChunk];
+};
+
+// Row/column tables of a polar tile; aliased onto the window region during set-up.
+struct PolarTables {
+    double rx[kMaxRows], ry[kMaxRows];
+    float rxh[kMaxRows], rxl[kMaxRows], ryh[kMaxRows], ryl[kMaxRows], dg[kMaxRows], psi[kMaxRows];
+    double cxd[kMaxCols], cyd[kMaxCols];
+    float cxh[kMaxCols], cxl[kMaxCols], cyh[kMaxCols], cyl[kMaxCols], dcs[kMaxCols], duu[kMaxCols];
+};
+
+struct SplitParams {
+    PulseInputs in;
+    float2* out;           // direct jobs: output image (pulse split s writes out + s * split_stride)
+    long long out_stride;
+    double K;          // k / 2pi (turns per metre)
+    double inv_dr;     // 1 / data_dr
+    double scale_w, inv_scale_w;
+    float Kf, inv_drf;
+    int chunk, wb;
+    int pulse_split;
+    long long split_stride;
+};
+
+struct Job {
+    PolarDesc g;          // polar grids
+    sarbp_lattice lat;    // lattices
+    const double* xyz;    // point lists
+    int npts;
+    int tile_r, tile_u, lc;
+    int p0, p1;
+    float2* out;
+    long long out_stride;
+};
+
+// ---- block reductions (256 threads) ---------------------------------------------
+template <int N>
+__device__ __forceinline__ void block_max(TileShared& S, float v[N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[i] = fmaxf(v[i], __shfl_xor_sync(0xffffffffu, v[i], o));
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) S.red[warp][i] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float m = S.red[0][i];
+#pragma unroll
+        for (int w = 1; w < 8; ++w) m = fmaxf(m, S.red[w][i]);
+        v[i] = m;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void block_sum4(TileShared& S, double v[4]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ double part[8][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) part[warp][i] = v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 4; ++i) {
+            double s = 0.0;
+            for (int w = 0; w < 8; ++w) s += part[w][i];
+            S.sum[i] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = S.sum[i];
+    __syncthreads();
+}
+
+__device__ __forceinline__ void set_quantum(TileShared& S, float bound, int bits) {
+    int e;
+    frexp((double)bound, &e);
+    S.scale_d = ldexp(1.0, e - bits);
+    S.inv_scale_d = ldexp(1.0, bits - e);
+}
+
+__device__ __forceinline__ void pixel_from_offsets(const TileShared& S, double ox, double oy, double oz, Pix& P) {
+    quantize(ox, S.scale_d, S.inv_scale_d, P.dxh, P.dxl);
+    quantize(oy, S.scale_d, S.inv_scale_d, P.dyh, P.dyl);
+    quantize(oz, S.scale_d, S.inv_scale_d, P.dzh, P.dzl);
+    P.dx = (float)ox;
+    P.dy = (float)oy;
+    P.dz = (float)oz;
+    P.d2 = P.dx * P.dx + P.dy * P.dy + P.dz * P.dz;
+}
+
+// ---- per-tile set-up: tile centre, quantum, per-pixel offsets -------------------
+// Polar tile: rows/cols of a polar grid window; separable FP64 row and column
+// tables give each pixel offset as an exact hi part plus an FP32 remainder.
+__device__ void setup_polar(const SplitParams& P, const Job& J, TileShared& S, PolarTables& T, Pix px[kPX],
+                            bool demodulate) {
+    const PolarDesc& g = J.g;
+    const int tid = threadIdx.x;
+    const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
+    const double oz = g.oz, side = (double)g.side;
+    const int i0 = g.win_r0 + J.tile_r + (rows_t >> 1);
+    const int j0 = g.win_u0 + J.tile_u + (cols_t >> 1);
+    const double rc = g.r0 + (double)i0 * g.dr;
+    const double gc = sqrt(fmax(0.0, rc * rc - oz * oz));
+    const double uc = g.u0 + (double)j0 * g.du;
+    const double cc = sqrt(fmax(0.0, 1.0 - uc * uc));
+    float m[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (tid < rows_t) {
+        const double r = g.r0 + (double)(g.win_r0 + J.tile_r + tid) * g.dr;
+        const double dg = sqrt(fmax(0.0, r * r - oz * oz)) - gc;
+        const double rx = side * dg * cc, ry = dg * uc;
+        T.rx[tid] = rx;
+        T.ry[tid] = ry;
+        T.dg[tid] = (float)dg;
+        const double t = -P.K * r;
+        T.psi[tid] = demodulate ? (float)(t - rint(t)) : 0.0f;
+        m[0] = (float)fabs(rx);
+        m[1] = (float)fabs(ry);
+        m[2] = (float)fabs(dg);
+    }
+    if (tid < cols_t) {
+        const double u = g.u0 + (double)(g.win_u0 + J.tile_u + tid) * g.du;
+        const double dc = sqrt(fmax(0.0, 1.0 - u * u)) - cc, du = u - uc;
+        const double cx = side * gc * dc, cy = gc * du;
+        T.cxd[tid] = cx;
+        T.cyd[tid] = cy;
+        T.dcs[tid] = (float)(side * dc);
+        T.duu[tid] = (float)du;
+        m[3] = (float)fabs(cx);
+        m[4] = (float)fabs(cy);
+        m[5] = (float)fabs(dc);
+        m[6] = (float)fabs(du);
+    }
+    block_max<7>(S, m);
+    // Bounds on |delta_x|, |delta_y| (slightly enlarged for the FP32 maxima).
+    const float bx = (m[0] + m[3] + m[2] * m[5]) * 1.0001f + 1e-6f;
+    const float by = (m[1] + m[4] + m[2] * m[6]) * 1.0001f + 1e-6f;
+    if (tid == 0) {
+        S.cx = g.ox + side * gc * cc;
+        S.cy = g.oy + gc * uc;
+        S.cz = 0.0;
+        S.rho = sqrt((double)bx * bx + (double)by * by);
+        set_quantum(S, fmaxf(bx, by), 12);
+    }
+    __syncthreads();
+    if (tid < rows_t) {
+        quantize(T.rx[tid], S.scale_d, S.inv_scale_d, T.rxh[tid], T.rxl[tid]);
+        quantize(T.ry[tid], S.scale_d, S.inv_scale_d, T.ryh[tid], T.ryl[tid]);
+    }
+    if (tid < cols_t) {
+        quantize(T.cxd[tid], S.scale_d, S.inv_scale_d, T.cxh[tid], T.cxl[tid]);
+        quantize(T.cyd[tid], S.scale_d, S.inv_scale_d, T.cyh[tid], T.cyl[tid]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = tid + kThreads * k;
+        const int row = p >> J.lc, col = p & (cols_t - 1);
+        Pix& q = px[k];
+        q.dxh = T.rxh[row] + T.cxh[col];  // exact: both multiples of the quantum
+        q.dyh = T.ryh[row] + T.cyh[col];
+        q.dxl = fmaf(T.dg[row], T.dcs[col], T.rxl[row] + T.cxl[col]);
+        q.dyl = fmaf(T.dg[row], T.duu[col], T.ryl[row] + T.cyl[col]);
+        q.dzh = q.dzl = q.dz = 0.0f;
+        q.dx = q.dxh + q.dxl;
+        q.dy = q.dyh + q.dyl;
+        q.d2 = q.dx * q.dx + q.dy * q.dy;
+        q.psi = T.psi[row];
+        q.ar = q.ai = 0.0f;
+    }
+    __syncthreads();  // the tables alias the window region
+}
+
+template <bool HAS_Z>
+__device__ void setup_lattice(const Job& J, TileShared& S, Pix px[kPX]) {
+    const sarbp_lattice& L = J.lat;
+    const int tid = threadIdx.x;
+    const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
+    const int hr = rows_t >> 1, hc = cols_t >> 1;
+    if (tid == 0) {
+        const double i0 = (double)(J.tile_r + hr), j0 = (double)(J.tile_u + hc);
+        S.cx = L.origin[0] + i0 * L.step_row[0] + j0 * L.step_col[0];
+        S.cy = L.origin[1] + i0 * L.step_row[1] + j0 * L.step_col[1];
+        S.cz = L.origin[2] + i0 * L.step_row[2] + j0 * L.step_col[2];
+        double b[3];
+        for (int c = 0; c < 3; ++c) b[c] = hr * fabs(L.step_row[c]) + hc * fabs(L.step_col[c]);
+        S.rho = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) * 1.0001 + 1e-6;
+        set_quantum(S, (float)(fmax(b[0], fmax(b[1], b[2])) * 1.0001 + 1e-6), HAS_Z ? 11 : 12);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = tid + kThreads * k;
+        const double di = (double)((p >> J.lc) - hr), dj = (double)((p & (cols_t - 1)) - hc);
+        Pix& q = px[k];
+        pixel_from_offsets(S, di * L.step_row[0] + dj * L.step_col[0], di * L.step_row[1] + dj * L.step_col[1],
+                           HAS_Z ? di * L.step_row[2] + dj * L.step_col[2] : 0.0, q);
+        q.psi = 0.0f;
+        q.ar = q.ai = 0.0f;
+    }
+}
+
+__device__ void setup_points(const Job& J, TileShared& S, Pix px[kPX]) {
+    const int tid = threadIdx.x;
+    double p3[kPX][3];
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int idx = J.tile_r + tid + kThreads * k;
+        const bool ok = idx < J.npts;
+        const int q = ok ? idx : J.tile_r;
+        p3[k][0] = J.xyz[3 * q];
+        p3[k][1] = J.xyz[3 * q + 1];
+        p3[k][2] = J.xyz[3 * q + 2];
+        if (ok) {
+            v[0] += p3[k][0];
+            v[1] += p3[k][1];
+            v[2] += p3[k][2];
+            v[3] += 1.0;
+        }
+    }
+    block_sum4(S, v);
+    const double cx = v[0] / v[3], cy = v[1] / v[3], cz = v[2] / v[3];
+    float m[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        m[0] = fmaxf(m[0], (float)fabs(p3[k][0] - cx));
+        m[1] = fmaxf(m[1], (float)fabs(p3[k][1] - cy));
+        m[2] = fmaxf(m[2], (float)fabs(p3[k][2] - cz));
+    }
+    block_max<3>(S, m);
+    if (tid == 0) {
+        S.cx = cx;
+        S.cy = cy;
+        S.cz = cz;
+        const double b0 = m[0] * 1.0001 + 1e-6, b1 = m[1] * 1.0001 + 1e-6, b2 = m[2] * 1.0001 + 1e-6;
+        S.rho = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+        set_quantum(S, (float)fmax(b0, fmax(b1, b2)), 11);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        Pix& q = px[k];
+        pixel_from_offsets(S, p3[k][0] - cx, p3[k][1] - cy, p3[k][2] - cz, q);
+        q.psi = 0.0f;
+        q.ar = q.ai = 0.0f;
+    }
+}
+
+// ---- the pulse loop ---------------------------------------------------------------
+template <bool HAS_Z>
+__device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __restrict__ rec,
+                                           const float4* __restrict__ win, int chn, Pix px[kPX]) {
+    const unsigned wbm1 = (unsigned)(P.wb - 1);
+    const float inv_dr = P.inv_drf, Kf = P.Kf;
+#pragma unroll 1
+    for (int nl = 0; nl < chn; ++nl) {
+        const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c;
+        float uz = 0.0f;
+        if (HAS_Z) uz = rec[nl].d.x;
+        const int cb = __float_as_int(rc.y);
+        const float4* wrow = win + (size_t)nl * P.wb * 2;
+#pragma unroll
+        for (int k = 0; k < kPX; ++k) {
+            Pix& q = px[k];
+            float L = fmaf(rb.x, q.dx, rb.y * q.dy);
+            if (HAS_Z) L = fmaf(uz, q.dz, L);
+            const float q2 = fmaf(-L, L, q.d2);
+            const float B = rcp_approx(fmaf(2.0f, L, rb.z));
+            const float e0 = q2 * B;
+            const float eps = fmaf(-e0 * e0, B, e0);
+            const float qp = fmaf(L + eps, inv_dr, rb.w);
+            const float tq = qp + kMagic;
+            const float s = qp - (tq - kMagic);
+            const unsigned j = min((unsigned)(__float_as_int(tq) - cb), wbm1);
+            const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+            const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+            const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+            float tb = ra.y * q.dyh;
+            if (HAS_Z) tb = fmaf(rc.z, q.dzh, tb);
+            tb = fmaf(ra.x, q.dxh, tb);
+            const float fb = tb - round_magic(tb);
+            float sm = fmaf(Kf, eps, rc.x);
+            sm = fmaf(ra.x, q.dxl, sm);
+            sm = fmaf(ra.y, q.dyl, sm);
+            sm = fmaf(ra.z, q.dx, sm);
+            sm = fmaf(ra.w, q.dy, sm);
+            if (HAS_Z) {
+                sm = fmaf(rc.z, q.dzl, sm);
+                sm = fmaf(rc.w, q.dz, sm);
+            }
+            const float tot = (fb + q.psi) + sm;
+            const float ang = (tot - round_magic(tot)) * kTwoPiF;
+            float sn, cs;
+            __sincosf(ang, &sn, &cs);
+            q.ar = fmaf(vr, cs, q.ar);
+            q.ar = fmaf(-vi, sn, q.ar);
+            q.ai = fmaf(vr, sn, q.ai);
+            q.ai = fmaf(vi, cs, q.ai);
+        }
+    }
+}
+
+// FP64 per-sample fallback for chunks whose windows do not fit (very large tiles).
+__device__ __forceinline__ void slow_chunk(const SplitParams& P, const TileShared& S, int c0, int chn, Pix px[kPX]) {
+    const PulseInputs& in = P.in;
+    for (int nl = 0; nl < chn; ++nl) {
+        const int n = c0 + nl;
+        const double pxn = in.pos[3 * n], pyn = in.pos[3 * n + 1], pzn = in.pos[3 * n + 2];
+        const double ph = in.phase[n] * kInvTwoPi;
+        const float a = (float)in.weight[n];
+        const float2* row = in.data + (size_t)n * in.samples;
+        for (int k = 0; k < kPX; ++k) {
+            Pix& q = px[k];
+            const double x = S.cx + ((double)q.dxh + (double)q.dxl) - pxn;
+            const double y = S.cy + ((double)q.dyh + (double)q.dyl) - pyn;
+            const double z = S.cz + ((double)q.dzh + (double)q.dzl) - pzn;
+            const double d = sqrt(x * x + y * y + z * z);
+            const double t = P.K * d + ph;
+            const float tot = (float)(t - rint(t)) + q.psi;
+            const float ang = (tot - round_magic(tot)) * kTwoPiF;
+            const double qq = (d - in.range_start) * P.inv_dr;
+            const double fl = floor(qq);
+            if (!(fl >= 1.0 && fl <= (double)(in.samples - 3))) continue;
+            const int i = (int)fl;
+            float w[4];
+            lagrange_centred((float)(qq - fl - 0.5), w);
+            float vr = 0.0f, vi = 0.0f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const float2 v = __ldg(row + i + b - 1);
+                vr = fmaf(w[b], v.x, vr);
+                vi = fmaf(w[b], v.y, vi);
+            }
+            vr *= a;
+            vi *= a;
+            float sn, cs;
+            __sincosf(ang, &sn, &cs);
+            q.ar = fmaf(vr, cs, q.ar);
+            q.ar = fmaf(-vi, sn, q.ar);
+            q.ai = fmaf(vr, sn, q.ai);
+            q.ai = fmaf(vi, cs, q.ai);
+        }
+    }
+}
+
+template <bool HAS_Z>
+__device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, Pix px[kPX]) {
+    const PulseInputs& in = P.in;
+    const int tid = threadIdx.x;
+    const int CH = P.chunk, WB = P.wb;
+    Rec* rec = reinterpret_cast<Rec*>(smem);
+    float4* win = reinterpret_cast<float4*>(smem + (size_t)CH * sizeof(Rec));
+    for (int c0 = J.p0; c0 < J.p1; c0 += CH) {
+        const int chn = min(CH, J.p1 - c0);
+        __syncthreads();
+        int bad = 0;
+        if (tid < chn) {
+            const int n = c0 + tid;
+            const double vx = S.cx - in.pos[3 * n], vy = S.cy - in.pos[3 * n + 1], vz = S.cz - in.pos[3 * n + 2];
+            const double R = sqrt(vx * vx + vy * vy + vz * vz);
+            const double iR = 1.0 / R;
+            const double ux = vx * iR, uy = vy * iR, uz = vz * iR;
+            const double t1 = P.K * R + in.phase[n] * kInvTwoPi;
+            const double Q = (R - in.range_start) * P.inv_dr;
+            const double I = floor(Q);
+            const double Fm = (Q - I) - 0.5;
+            const double wing = (S.rho + S.rho * S.rho * iR) * fabs(P.inv_dr) + 0.01;
+            const double lo = floor(Fm - wing), hi = ceil(Fm + wing);
+            bad = !(R > 0.0) || !(fabs(Q) < 1.0e9) || !(hi - lo + 1.0 <= (double)WB);
+            const int bo = bad ? 0 : (int)lo;
+            S.base[tid] = bad ? 0 : (int)I + bo;
+            S.wt[tid] = (float)in.weight[n];
+            Rec r;
+            quantize(P.K * ux, P.scale_w, P.inv_scale_w, r.a.x, r.a.z);
+            quantize(P.K * uy, P.scale_w, P.inv_scale_w, r.a.y, r.a.w);
+            quantize(P.K * uz, P.scale_w, P.inv_scale_w, r.c.z, r.c.w);
+            r.b = make_float4((float)ux, (float)uy, (float)(2.0 * R), (float)Fm);
+            r.c.x = (float)(t1 - rint(t1));
+            r.c.y = __int_as_float(kMagicBits + bo);
+            r.d = make_float4((float)uz, 0.0f, 0.0f, 0.0f);
+            rec[tid] = r;
+        }
+        const int slow = __syncthreads_or(bad);
+        if (!slow) {
+            const int total = chn * WB;
+            for (int e = tid; e < total; e += kThreads) {
+                const int nl = e / WB;
+                const int j = e - nl * WB;
+                const long long gbin = (long long)S.base[nl] + j;
+                float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
+                if (gbin >= 1 && gbin <= (long long)in.samples - 3) {
+                    const float2* row = in.data + (size_t)(c0 + nl) * in.samples + gbin;
+                    cubic_coefficients(__ldg(row - 1), __ldg(row), __ldg(row + 1), __ldg(row + 2), S.wt[nl], c01,
+                                       c23);
+                }
+                win[2 * e] = c01;
+                win[2 * e + 1] = c23;
+            }
+        }
+        __syncthreads();
+        if (!slow) {
+            fast_chunk<HAS_Z>(P, rec, win, chn, px);
+        } else {
+            slow_chunk(P, S, c0, chn, px);
+        }
+    }
+}
+
+
+// ---- output ----------------------------------------------------------------------
+__device__ __forceinline__ void store_window(const Job& J, int win_nr, int win_nu, const Pix px[kPX], float2* out,
+                                             long long stride) {
+    const int cols_t = 1 << J.lc;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = threadIdx.x + kThreads * k;
+        const int wr = J.tile_r + (p >> J.lc), wu = J.tile_u + (p & (cols_t - 1));
+        if (wr < win_nr && wu < win_nu) out[(long long)wr * stride + wu] = make_float2(px[k].ar, px[k].ai);
+    }
+}
+
+__device__ __forceinline__ void split_range(int p0, int p1, int parts, int part, int& b, int& e) {
+    const long long len = (long long)p1 - p0;
+    b = p0 + (int)(len * part / parts);
+    e = p0 + (int)(len * (part + 1) / parts);
+}
+
+__device__ __forceinline__ void tile_of(int index, int win_nu, int lc, int& tile_r, int& tile_u) {
+    const int cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
+    const int tiles_u = (win_nu + cols_t - 1) / cols_t;
+    tile_r = (index / tiles_u) * rows_t;
+    tile_u = (index % tiles_u) * cols_t;
+}
+
+// ---- direct BP kernels --------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 2) split_polar_kernel(SplitParams P, PolarDesc g) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    Job J;
+    J.g = g;
+    J.lc = g.tile_lc;
+    tile_of(blockIdx.x, g.win_nu, J.lc, J.tile_r, J.tile_u);
+    split_range(g.a, g.b, P.pulse_split, blockIdx.y, J.p0, J.p1);
+    Pix px[kPX];
+    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)P.chunk * sizeof(Rec));
+    setup_polar(P, J, S, T, px, true);
+    pulse_loop<false>(P, J, S, smem, px);
+    store_window(J, g.win_nr, g.win_nu, px, P.out + blockIdx.y * P.split_stride, P.out_stride);
+}
+
+template <bool HAS_Z>
+__global__ void __launch_bounds__(kThreads, 2) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    Job J;
+    J.lat = lat;
+    J.lc = lc;
+    tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
+    split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, J.p0, J.p1);
+    Pix px[kPX];
+    setup_lattice<HAS_Z>(J, S, px);
+    pulse_loop<HAS_Z>(P, J, S, smem, px);
+    store_window(J, lat.rows, lat.cols, px, P.out + blockIdx.y * P.split_stride, lat.cols);
+}
+
+__global__ void __launch_bounds__(kThreads, 2) split_points_kernel(SplitParams P, const double* __restrict__ xyz,
+                                                                   int npts) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    Job J;
+    J.xyz = xyz;
+    J.npts = npts;
+    J.lc = 0;
+    J.tile_r = blockIdx.x * kSplitTilePixels;
+    J.tile_u = 0;
+    split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, J.p0, J.p1);
+    Pix px[kPX];
+    setup_points(J, S, px);
+    pulse_loop<true>(P, J, S, smem, px);
+    float2* out = P.out + blockIdx.y * P.split_stride;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int idx = J.tile_r + threadIdx.x + kThreads * k;
+        if (idx < npts) out[idx] = make_float2(px[k].ar, px[k].ai);
+    }
+}
+
+// ---- FFBP: leaves ---------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 2) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+                                                                 const TileItem* __restrict__ items,
+                                                                 float2* __restrict__ arena, float2* root_out,
+                                                                 int root) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    const TileItem it = items[blockIdx.x];
+    Job J;
+    J.g = nodes[it.node];
+    J.lc = J.g.tile_lc;
+    J.tile_r = it.tile_r;
+    J.tile_u = it.tile_u;
+    J.p0 = J.g.a;
+    J.p1 = J.g.b;
+    Pix px[kPX];
+    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)P.chunk * sizeof(Rec));
+    setup_polar(P, J, S, T, px, true);
+    pulse_loop<false>(P, J, S, smem, px);
+    float2* dst = it.node == root ? root_out : arena + J.g.out_offset;
+    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+}
+
+// ---- FFBP: merges (both child regrids of one parent tile) --------------------------------
+struct ChildRec {
+    float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y
+    float4 b;  // u.x, u.y, 2 RR, frac(Qr) - 1/2
+    float4 c;  // Phi, h.x, h.y, 2 G
+    float4 d;  // G, frac(Qu) - 1/2
+    float inv_sdr, inv_sdu;
+    int ir0, iu0, snr, snu;
+    const float2* img;
+};
+
+__device__ __forceinline__ void child_record(const SplitParams& P, const TileShared& S, const PolarDesc& c,
+                                             const float2* img, ChildRec& R) {
+    const double vx = S.cx - c.ox, vy = S.cy - c.oy, vz = S.cz - c.oz;
+    const double g2 = vx * vx + vy * vy;
+    const double G = sqrt(g2);
+    const double RR = sqrt(g2 + vz * vz);
+    const double ux = vx / RR, uy = vy / RR;
+    const double t1 = P.K * RR;
+    const double qr = (RR - c.r0) / c.dr;
+    const double ir = floor(qr);
+    const double hx = vx / G, hy = vy / G;
+    const double qu = (hy - c.u0) / c.du;
+    const double iu = floor(qu);
+    quantize(P.K * ux, P.scale_w, P.inv_scale_w, R.a.x, R.a.z);
+    quantize(P.K * uy, P.scale_w, P.inv_scale_w, R.a.y, R.a.w);
+    R.b = make_float4((float)ux, (float)uy, (float)(2.0 * RR), (float)(qr - ir - 0.5));
+    R.c = make_float4((float)(t1 - rint(t1)), (float)hx, (float)hy, (float)(2.0 * G));
+    R.d = make_float4((float)G, (float)(qu - iu - 0.5), 0.0f, 0.0f);
+    R.inv_sdr = (float)(1.0 / c.dr);
+    R.inv_sdu = (float)(1.0 / c.du);
+    const bool ok = fabs(ir) < 1.0e9 && fabs(iu) < 1.0e9 && G > 0.0;
+    R.ir0 = ok ? (int)ir : -(1 << 30);
+    R.iu0 = ok ? (int)iu : -(1 << 30);
+    R.snr = c.nr;
+    R.snu = c.nu;
+    R.img = img;
+}
+
+__device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildRec& R, const Pix& q) {
+    const float L = fmaf(R.b.x, q.dx, R.b.y * q.dy);
+    const float q2 = fmaf(-L, L, q.d2);
+    const float B = rcp_approx(fmaf(2.0f, L, R.b.z));
+    const float e0 = q2 * B;
+    const float eps = fmaf(-e0 * e0, B, e0);
+    const float qr = fmaf(L + eps, R.inv_sdr, R.b.w);
+    const float tr = qr + kMagic;
+    const float sr = qr - (tr - kMagic);
+    const int ir = R.ir0 + (__float_as_int(tr) - kMagicBits);
+    const float Lh = fmaf(R.c.y, q.dx, R.c.z * q.dy);
+    const float q2h = fmaf(-Lh, Lh, q.d2);
+    const float Bh = rcp_approx(fmaf(2.0f, Lh, R.c.w));
+    const float eh = q2h * Bh;
+    const float dG = Lh + fmaf(-eh * eh, Bh, eh);
+    const float gp = R.d.x + dG;
+    const float duu = fmaf(-R.c.z, dG, q.dy) * rcp_approx(gp);
+    const float qu = fmaf(duu, R.inv_sdu, R.d.y);
+    const float tu = qu + kMagic;
+    const float su = qu - (tu - kMagic);
+    const int iu = R.iu0 + (__float_as_int(tu) - kMagicBits);
+    float vr = 0.0f, vi = 0.0f;
+    if (ir >= 1 && ir <= R.snr - 3 && iu >= 1 && iu <= R.snu - 3 && gp > 0.0f) {
+        float wr[4], wu[4];
+        lagrange_centred(sr, wr);
+        lagrange_centred(su, wu);
+        const float2* base = R.img + (size_t)(ir - 1) * R.snu + (iu - 1);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const float2* row = base + (size_t)a * R.snu;
+            const float2 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2), x3 = __ldg(row + 3);
+            float rr = wu[0] * x0.x, ri = wu[0] * x0.y;
+            rr = fmaf(wu[1], x1.x, rr);
+            ri = fmaf(wu[1], x1.y, ri);
+            rr = fmaf(wu[2], x2.x, rr);
+            ri = fmaf(wu[2], x2.y, ri);
+            rr = fmaf(wu[3], x3.x, rr);
+            ri = fmaf(wu[3], x3.y, ri);
+            vr = fmaf(wr[a], rr, vr);
+            vi = fmaf(wr[a], ri, vi);
+        }
+    }
+    const float tb = fmaf(R.a.x, q.dxh, R.a.y * q.dyh);
+    const float fb = tb - round_magic(tb);
+    float sm = fmaf(P.Kf, eps, R.c.x);
+    sm = fmaf(R.a.x, q.dxl, sm);
+    sm = fmaf(R.a.y, q.dyl, sm);
+    sm = fmaf(R.a.z, q.dx, sm);
+    sm = fmaf(R.a.w, q.dy, sm);
+    const float tot = (fb + q.psi) + sm;
+    const float ang = (tot - round_magic(tot)) * kTwoPiF;
+    float sn, cs;
+    __sincosf(ang, &sn, &cs);
+    return make_float2(vr * cs - vi * sn, vr * sn + vi * cs);
+}
+
+__global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+                                                                  const TileItem* __restrict__ items,
+                                                                  float2* __restrict__ arena, float2* root_out,
+                                                                  int root) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    __shared__ ChildRec C[2];
+    const TileItem it = items[blockIdx.x];
+    Job J;
+    J.g = nodes[it.node];
+    J.lc = J.g.tile_lc;
+    J.tile_r = it.tile_r;
+    J.tile_u = it.tile_u;
+    Pix px[kPX];
+    PolarTables& T = *reinterpret_cast<PolarTables*>(smem);
+    setup_polar(P, J, S, T, px, true);
+    if (threadIdx.x < 2) {
+        const int child = threadIdx.x == 0 ? J.g.left : J.g.right;
+        const PolarDesc c = nodes[child];
+        child_record(P, S, c, arena + c.out_offset, C[threadIdx.x]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const float2 a = child_value(P, C[0], px[k]);
+        const float2 b = child_value(P, C[1], px[k]);
+        px[k].ar = __fadd_rn(a.x, b.x);
+        px[k].ai = __fadd_rn(a.y, b.y);
+    }
+    float2* dst = it.node == root ? root_out : arena + J.g.out_offset;
+    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+}
+
+SplitParams make_params(const PulseInputs& in, int chunk, int wb, int pulse_split) {
+    SplitParams P;
+    P.in = in;
+    P.out = nullptr;
+    P.out_stride = 0;
+    P.K = in.k * kInvTwoPi;
+    P.inv_dr = in.data_dr != 0.0 ? 1.0 / in.data_dr : 0.0;
+    int e = 0;
+    frexp(fabs(P.K) > 0.0 ? fabs(P.K) : 1e-30, &e);
+    P.scale_w = ldexp(1.0, e - 10);
+    P.inv_scale_w = ldexp(1.0, 10 - e);
+    P.Kf = (float)P.K;
+    P.inv_drf = (float)P.inv_dr;
+    P.chunk = chunk;
+    P.wb = wb;
+    P.pulse_split = pulse_split;
+    P.split_stride = 0;
+    return P;
+}
+
+size_t dynamic_smem(int chunk, int wb, bool polar) {
+    size_t win = (size_t)chunk * wb * 32;
+    if (polar && win < sizeof(PolarTables)) win = sizeof(PolarTables);
+    return (size_t)chunk * sizeof(Rec) + win;
+}
+
+template <class K>
+int prepare(K kernel, size_t smem) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    }
+    return SARBP_OK;
+}
+
+int tiles_of(int nr, int nu, int lc) {
+    const int cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
+    return ((nr + rows_t - 1) / rows_t) * ((nu + cols_t - 1) / cols_t);
+}
+
+}  // namespace
+
+int split_window_bins(double radius, double data_dr) {
+    const double wing = (radius + radius * radius / 100.0) / fabs(data_dr) + 0.01;
+    return (int)ceil(2.0 * wing) + 4;
+}
+
+int split_chunk_for(int window_bins, int requested) {
+    int ch = requested > 0 ? requested : kMaxChunk;
+    if (ch > kMaxChunk) ch = kMaxChunk;
+    const int fit = kWindowBudget / (window_bins * 32 > 0 ? window_bins * 32 : 32);
+    if (ch > fit) ch = fit;
+    return ch < 1 ? 1 : ch;
+}
+
+int split_polar_tile_lc(const PolarDesc& g, double* radius) {
+    // Ground displacement per range row <= dr * r / g; per angle column <= du * g / sqrt(1 - u^2).
+    const double rmin = g.r0 + g.win_r0 * g.dr, rmax = g.r0 + (g.win_r0 + g.win_nr - 1) * g.dr;
+    const double gmin = sqrt(fmax(1e-6, rmin * rmin - g.oz * g.oz));
+    const double gmax = sqrt(fmax(1e-6, rmax * rmax - g.oz * g.oz));
+    const double ua = fabs(g.u0 + g.win_u0 * g.du), ub = fabs(g.u0 + (g.win_u0 + g.win_nu - 1) * g.du);
+    const double cmin = sqrt(fmax(1e-6, 1.0 - fmax(ua, ub) * fmax(ua, ub)));
+    const double per_row = fabs(g.dr) * fmax(rmin, rmax) / gmin;
+    const double per_col = fabs(g.du) * gmax / cmin;
+    int best = 5;
+    double best_r = 1e300;
+    for (int lc = 2; lc <= 5; ++lc) {
+        const double er = (kSplitTilePixels >> lc) * per_row, eu = (1 << lc) * per_col;
+        const double rad = 0.5 * sqrt(er * er + eu * eu) * 1.05;
+        if (rad < best_r) {
+            best_r = rad;
+            best = lc;
+        }
+    }
+    if (radius) *radius = best_r;
+    return best;
+}
+
+int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_split, int chunk, int window_bins,
+                       float2* out, long long out_stride, long long split_stride, cudaStream_t s) {
+    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    P.out = out;
+    P.out_stride = out_stride;
+    P.split_stride = split_stride;
+    const size_t smem = dynamic_smem(chunk, window_bins, true);
+    if (int st = prepare(split_polar_kernel, smem)) return st;
+    dim3 grid(tiles_of(g.win_nr, g.win_nu, g.tile_lc), pulse_split);
+    split_polar_kernel<<<grid, kThreads, smem, s>>>(P, g);
+    note_launches(1);
+    return check_launch("split_polar");
+}
+
+int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk, int window_bins,
+                         float2* out, long long split_stride, cudaStream_t s) {
+    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    P.out = out;
+    P.split_stride = split_stride;
+    const int lc = 5;
+    const size_t smem = dynamic_smem(chunk, window_bins, false);
+    dim3 grid(tiles_of(lat.rows, lat.cols, lc), pulse_split);
+    const bool has_z = lat.step_row[2] != 0.0 || lat.step_col[2] != 0.0;
+    if (has_z) {
+        if (int st = prepare(split_lattice_kernel<true>, smem)) return st;
+        split_lattice_kernel<true><<<grid, kThreads, smem, s>>>(P, lat, lc);
+    } else {
+        if (int st = prepare(split_lattice_kernel<false>, smem)) return st;
+        split_lattice_kernel<false><<<grid, kThreads, smem, s>>>(P, lat, lc);
+    }
+    note_launches(1);
+    return check_launch("split_lattice");
+}
+
+int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
+                        int window_bins, float2* out, long long split_stride, cudaStream_t s) {
+    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    P.out = out;
+    P.split_stride = split_stride;
+    const size_t smem = dynamic_smem(chunk, window_bins, false);
+    if (int st = prepare(split_points_kernel, smem)) return st;
+    dim3 grid((npts + kSplitTilePixels - 1) / kSplitTilePixels, pulse_split);
+    split_points_kernel<<<grid, kThreads, smem, s>>>(P, xyz, npts);
+    note_launches(1);
+    return check_launch("split_points");
+}
+
+int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
+                             int chunk, int window_bins, float2* arena, float2* root_out, int root, cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    SplitParams P = make_params(in, chunk, window_bins, 1);
+    const size_t smem = dynamic_smem(chunk, window_bins, true);
+    if (int st = prepare(split_leaf_kernel, smem)) return st;
+    split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, arena, root_out, root);
+    note_launches(1);
+    return check_launch("split_ffbp_leaves");
+}
+
+int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems, float2* arena,
+                             float2* root_out, int root, cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    PulseInputs none{};
+    none.k = k;
+    none.data_dr = 1.0;
+    SplitParams P = make_params(none, 0, 0, 1);
+    const size_t smem = sizeof(PolarTables);
+    if (int st = prepare(split_merge_kernel, smem)) return st;
+    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, arena, root_out, root);
+    note_launches(1);
+    return check_launch("split_ffbp_merges");
+}
+
+}  // namespace sarbp

@@ -1,0 +1,210 @@
+/*
+ * sarbp.h - C ABI of the GB300 (sm_103a) SAR back-projection library.
+ *
+ * Direct back-projection (BP) and polar fast factorized back-projection
+ * (FFBP): range-compressed complex64 pulses, per-pulse antenna positions and
+ * an image grid go in, a complex64 image comes out.  This is the boundary the
+ * Python host (bp_project_gb300) binds with ctypes; any other host can bind it
+ * the same way.  No torch or CUDA C++ types appear in the signatures.
+ *
+ * Conventions (shared with the reference fast_bp path):
+ *   - All array arguments are DEVICE pointers owned by the caller.  Complex
+ *     arrays are interleaved float pairs (complex64) unless stated otherwise.
+ *   - data is C-contiguous complex64 [pulses, samples]; pos is float64
+ *     [pulses, 3] (x cross-track, y along-track, z height); weight and phase
+ *     are float64 [pulses].  range_start (m) is the range of sample 0, data_dr
+ *     (m) the sample spacing, k the signed two-way wavenumber 4*pi*fc/c.
+ *   - Range interpolation is the reference's four-point Lagrange sample1
+ *     (fast_bp/ffbp.py:17-29): zero unless every tap lies inside the row.
+ *   - Polar grids: pixel (ir, iu) sits at r = r0 + ir*dr (slant range from the
+ *     grid origin), u = u0 + iu*du (sine of the horizontal angle);
+ *     x = ox + side*g*sqrt(1-u^2), y = oy + g*u, z = 0 with g = sqrt(r^2-oz^2).
+ *     Polar images are demodulated by exp(-j*k*r) (fast_bp/ffbp.py:58-76).
+ *   - Every call only enqueues work on `stream` (a cudaStream_t, NULL = the
+ *     legacy default stream); none synchronises, allocates device memory or
+ *     copies between host and device, except sarbp_ffbp_bind which uploads
+ *     the plan tables.  Calls are safe to capture in a CUDA graph, except
+ *     sarbp_ffbp_bind.
+ *   - Return value: SARBP_OK or an error code; sarbp_last_error() returns a
+ *     thread-local message for the most recent failure in the calling thread.
+ *
+ * Precision modes:
+ *   SARBP_FP64  FP64 geometry, interpolation, phase and accumulation
+ *   SARBP_FP32  FP32 everything (the reference's fp32 policy)
+ *   SARBP_MIXED FP64 geometry and phase, FP32 interpolation and accumulation
+ *   SARBP_SPLIT FP32 arithmetic with FP64 only per (pixel tile, pulse) and per
+ *               tile: tile-centre ranges in FP64, per-pixel range offsets as
+ *               exact split products, phase reduced in turns before a hardware
+ *               sin/cos.  Relative error vs FP64 is ~1e-6 (stated per image
+ *               by the tests); this is the fast path.
+ * The first three follow the reference's MODES (fast_bp/gpu_backend.py:57,
+ * gpu/kernels.cu:1-6).
+ */
+#ifndef SARBP_H
+#define SARBP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SARBP_ABI_VERSION 1
+
+enum sarbp_status {
+    SARBP_OK = 0,
+    SARBP_ERR_VALUE = 1,       /* invalid argument value or shape (ValueError)        */
+    SARBP_ERR_TYPE = 2,        /* null pointer / misaligned array (TypeError)         */
+    SARBP_ERR_WORKSPACE = 3,   /* workspace missing or too small (ValueError)        */
+    SARBP_ERR_CUDA = 4,        /* CUDA runtime error (RuntimeError)                  */
+    SARBP_ERR_PLAN = 5,        /* FFBP plan inconsistent or not bound (RuntimeError) */
+    SARBP_ERR_ENVELOPE = 6     /* geometry outside the split-precision envelope      */
+};
+
+enum sarbp_mode { SARBP_FP64 = 0, SARBP_FP32 = 1, SARBP_MIXED = 2, SARBP_SPLIT = 3 };
+
+/* Polar image grid (fast_bp/gpu_backend.py:60-78 NodePlan geometry). */
+typedef struct sarbp_polar_grid {
+    double origin[3];
+    double r0, dr;
+    double u0, du;
+    int32_t nr, nu;
+    int32_t side;     /* +1 / -1 look side */
+    int32_t reserved;
+} sarbp_polar_grid;
+
+/* Affine pixel lattice: pixel (i, j) at origin + i*step_row + j*step_col,
+ * image [rows, cols].  Equivalent to backproject_points on the lattice points. */
+typedef struct sarbp_lattice {
+    double origin[3];
+    double step_row[3];
+    double step_col[3];
+    int32_t rows, cols;
+} sarbp_lattice;
+
+/* One FFBP tree node (fast_bp/gpu_backend.py:60-78).  Nodes are given in
+ * pre-order; left/right index children, -1 for leaves which back-project
+ * pulses [a, b). */
+typedef struct sarbp_ffbp_node {
+    double origin[3];
+    double r0, dr, u0, du;
+    int32_t nr, nu;
+    int32_t a, b;
+    int32_t left, right;
+    int32_t side;
+    int32_t reserved;
+} sarbp_ffbp_node;
+
+typedef struct sarbp_ffbp_plan sarbp_ffbp_plan;
+
+/* ---- library information -------------------------------------------------- */
+const char* sarbp_version(void);
+int sarbp_abi_version(void);
+const char* sarbp_status_string(int status);
+const char* sarbp_last_error(void);
+/* Kernels this library launched since load (all entry points), for launch accounting. */
+uint64_t sarbp_launch_count(void);
+
+/* ---- direct back-projection ----------------------------------------------- */
+
+/* Workspace bytes sarbp_direct_polar needs for these arguments (0 if none).
+ * pulse_split > 1 splits the aperture over that many CTAs per pixel tile and
+ * sums the partial images in fixed order (scratch: pulse_split images). */
+size_t sarbp_direct_polar_workspace(int mode, const sarbp_polar_grid* grid, int pulses, int pulse_split);
+
+/* Direct BP of all pulses onto a polar grid; out is complex64 [nr, nu].
+ * Replaces CudaBaseline.run_direct (fast_bp/gpu_backend.py:471-555) and its
+ * direct_chunk_{fp64,fp32,mixed} + cast_double2_to_float2 launches
+ * (gpu/kernels.cu:240-339, :439-444); also the arithmetic of
+ * bp_polar_{fp64,fp32,mixed} (gpu/kernels.cu:139-238) and ffbp.bp_polar
+ * (ffbp.py:58-76).  chunk_pulses is the shared-memory pulse chunk (the
+ * reference's --chunk-pulses, gpu_baseline.py:413); results do not depend on it. */
+int sarbp_direct_polar(const float* data, int pulses, int samples, const double* pos,
+                       const double* weight, const double* phase, const sarbp_polar_grid* grid,
+                       double range_start, double data_dr, double k, int mode, int chunk_pulses,
+                       int pulse_split, float* out, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* Direct BP at arbitrary points xyz float64 [npts, 3]; out complex64 [npts].
+ * Replaces ffbp.backproject_points (fast_bp/ffbp.py:43-55): phase k*r + phase[n],
+ * not demodulated.  SPLIT mode groups consecutive points into tiles of 1024;
+ * callers get the best speed with spatially coherent point order. */
+size_t sarbp_backproject_points_workspace(int mode, int npts, int pulse_split);
+int sarbp_backproject_points(const float* data, int pulses, int samples, const double* pos,
+                             const double* weight, const double* phase, const double* xyz, int npts,
+                             double range_start, double data_dr, double k, int mode, int pulse_split,
+                             float* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Direct BP on an affine lattice (backproject_points semantics); out [rows, cols]. */
+size_t sarbp_backproject_lattice_workspace(int mode, const sarbp_lattice* lattice, int pulse_split);
+int sarbp_backproject_lattice(const float* data, int pulses, int samples, const double* pos,
+                              const double* weight, const double* phase, const sarbp_lattice* lattice,
+                              double range_start, double data_dr, double k, int mode, int pulse_split,
+                              float* out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- FFBP building blocks (eager schedule) -------------------------------- */
+
+/* Child polar image -> parent polar grid with 4x4 Lagrange and exp(j k (rr-r)).
+ * Replaces regrid_{fp64,fp32,mixed} (gpu/kernels.cu:341-429) / ffbp.regrid
+ * (ffbp.py:79-95).  out complex64 [dst.nr, dst.nu]. */
+int sarbp_regrid(const float* image, const sarbp_polar_grid* src, const sarbp_polar_grid* dst,
+                 double k, int mode, float* out, void* stream);
+
+/* Both child regrids rounded to complex64, then added: merge_regrid_*
+ * (gpu/resident_kernels.cu:35-157). */
+int sarbp_merge_regrid(const float* left, const sarbp_polar_grid* left_grid, const float* right,
+                       const sarbp_polar_grid* right_grid, const sarbp_polar_grid* dst, double k,
+                       int mode, float* out, void* stream);
+
+/* left += right over n complex64 values: add_float2_inplace (gpu/kernels.cu:431-437). */
+int sarbp_add_inplace(float* left, const float* right, int64_t n, void* stream);
+/* complex128 -> complex64: cast_double2_to_float2 (gpu/kernels.cu:439-444). */
+int sarbp_cast_c128_to_c64(const double* in, float* out, int64_t n, void* stream);
+/* Root guard crop: crop_float2 (gpu/kernels.cu:446-454). out [nr, nu] = in[r_begin:, u_begin:]. */
+int sarbp_crop(const float* in, int src_nu, int r_begin, int u_begin, int nr, int nu, float* out,
+               void* stream);
+
+/* ---- FFBP programs (level-batched, preallocated) -------------------------- */
+
+/* Replaces ResidentProgram(algorithm='ffbp') / BatchedResidentProgram
+ * (fast_bp/resident_backend.py:24-319, batched_resident_backend.py:23-157):
+ * one launch for all leaves, one per tree height, the root crop fused into the
+ * last merge.  create/destroy are host-only; bind uploads the tables into the
+ * caller's workspace (synchronous w.r.t. stream); execute only launches. */
+int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r0, int crop_u0,
+                           int crop_nr, int crop_nu, int mode, sarbp_ffbp_plan** plan);
+void sarbp_ffbp_plan_destroy(sarbp_ffbp_plan* plan);
+size_t sarbp_ffbp_workspace_bytes(const sarbp_ffbp_plan* plan);
+int sarbp_ffbp_launch_count(const sarbp_ffbp_plan* plan);
+int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_bytes, void* stream);
+int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulses, int samples,
+                       const double* pos, const double* weight, const double* phase, double range_start,
+                       double data_dr, double k, float* out, void* stream);
+
+/* ---- polar -> Cartesian and autofocus helpers ------------------------------- */
+
+/* ffbp.evaluate_image (ffbp.py:189-198): sample2 of a polar image at ground
+ * points xyz [npts, 3] (z ignored) times exp(j k r).  FP64 geometry and phase. */
+int sarbp_evaluate_image(const float* image, const sarbp_polar_grid* grid, const double* xyz, int npts,
+                         double k, float* out, void* stream);
+
+/* ffbp.target_contributions (ffbp.py:201-211): out[p, n] = sample1 * exp(j k r),
+ * complex64 [npts, pulses]; FP64 geometry and phase. */
+int sarbp_target_contributions(const float* data, int pulses, int samples, const double* pos,
+                               const double* xyz, int npts, double range_start, double data_dr, double k,
+                               float* out, void* stream);
+
+/* ---- phase look-up-table probe (gpu/precision_probe.cu:106-164) ------------ */
+int sarbp_fill_range_phase_lut(int samples, double range_start, double data_dr, double k, float* lut,
+                               void* stream);
+int sarbp_direct_polar_lut(const float* data, int pulses, int samples, const double* pos,
+                           const double* weight, const double* phase, const sarbp_polar_grid* grid,
+                           double range_start, double data_dr, double k, const float* lut, float* out,
+                           void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SARBP_H */

@@ -1,0 +1,147 @@
+"""Host-side checks that need no GPU: the C ABI loads and validates, the planner is bit-exact."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from bp_project_gb300 import build
+    build.build()
+    from bp_project_gb300 import _native
+    return _native
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "sarbp.h").read_text()
+    return sorted(set(re.findall(r"\b(sarbp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    handle = lib.load()
+    declared = _declared_symbols()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(handle, name), name
+        assert name in lib.SIGNATURES, f"{name} has no ctypes signature"
+    assert handle.sarbp_abi_version() == 1
+    assert b"sm_103a" in handle.sarbp_version()
+
+
+def test_status_mapping(lib):
+    with pytest.raises(ValueError):
+        lib.check(lib.SARBP_ERR_VALUE, "x")
+    with pytest.raises(TypeError):
+        lib.check(lib.SARBP_ERR_TYPE, "x")
+    with pytest.raises(RuntimeError):
+        lib.check(lib.SARBP_ERR_CUDA, "x")
+    lib.check(lib.SARBP_OK)
+
+
+def test_capi_rejects_bad_arguments_before_touching_the_gpu(lib):
+    h = lib.load()
+    g = lib.polar_grid((0, 0, 10), 100.0, 0.5, 16, -0.1, 0.01, 16, 1)
+    fake = ctypes.c_void_p(0x10000)  # never dereferenced: validation fails first
+    args = [fake, 8, 64, fake, fake, fake, ctypes.byref(g), 90.0, 0.5, -50.0]
+    assert h.sarbp_direct_polar(None, 8, 64, fake, fake, fake, ctypes.byref(g), 90.0, 0.5, -50.0, 3, 64, 1, fake,
+                                None, 0, None) == lib.SARBP_ERR_TYPE
+    assert h.sarbp_direct_polar(*args, 7, 64, 1, fake, None, 0, None) == lib.SARBP_ERR_VALUE       # mode
+    assert h.sarbp_direct_polar(*args, 3, 0, 1, fake, None, 0, None) == lib.SARBP_ERR_VALUE        # chunk
+    assert h.sarbp_direct_polar(*args, 3, 64, 9, fake, None, 0, None) == lib.SARBP_ERR_VALUE       # split > pulses
+    assert h.sarbp_direct_polar(*args, 3, 64, 4, fake, None, 0, None) == lib.SARBP_ERR_WORKSPACE   # no scratch
+    assert b"workspace" in h.sarbp_last_error()
+    empty = lib.polar_grid((0, 0, 10), 100.0, 0.5, 0, -0.1, 0.01, 16, 1)
+    assert h.sarbp_direct_polar(fake, 8, 64, fake, fake, fake, ctypes.byref(empty), 90.0, 0.5, -50.0, 3, 64, 1, fake,
+                                None, 0, None) == lib.SARBP_ERR_VALUE
+    assert b"empty image grids are unsupported" in h.sarbp_last_error()
+    bad_side = lib.polar_grid((0, 0, 10), 100.0, 0.5, 4, -0.1, 0.01, 4, 0)
+    assert h.sarbp_regrid(fake, ctypes.byref(bad_side), ctypes.byref(g), 1.0, 0, fake, None) == lib.SARBP_ERR_VALUE
+    nan_grid = lib.polar_grid((0, 0, 10), float("nan"), 0.5, 4, -0.1, 0.01, 4, 1)
+    assert h.sarbp_evaluate_image(fake, ctypes.byref(nan_grid), fake, 4, 1.0, fake, None) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_backproject_points(fake, 8, 64, fake, fake, fake, fake, 0, 90.0, 0.5, 1.0, 3, 1, fake, None, 0,
+                                      None) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_ffbp_execute(None, fake, 8, 64, fake, fake, fake, 90.0, 0.5, 1.0, fake, None) == lib.SARBP_ERR_TYPE
+    assert h.sarbp_direct_polar_workspace(3, ctypes.byref(g), 8, 4) == 4 * 16 * 16 * 8
+
+
+def _node_array(lib, plan):
+    nodes = plan.nodes()
+    arr = (lib.FFBPNode * len(nodes))()
+    for i, n in enumerate(nodes):
+        e = arr[i]
+        e.origin[:] = list(n.origin)
+        e.r0, e.dr, e.u0, e.du = n.r0, n.dr, n.u0, n.du
+        e.nr, e.nu, e.side, e.a, e.b = n.nr, n.nu, n.side, n.a, n.b
+        e.left = -1 if n.left is None else n.left.index
+        e.right = -1 if n.right is None else n.right.index
+    return arr
+
+
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+def test_ffbp_plan_object_on_host(golden, lib, mode):
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    g = golden("plans")
+    fc, rmin, rmax, umin, umax, side, leaf, rs, osr = g["c1_args"]
+    plan = build_ffbp_plan(g["c1_position"], fc, (rmin, rmax, umin, umax), side=int(side), leaf_size=int(leaf),
+                           range_spacing=rs, angular_oversample=osr)
+    arr = _node_array(lib, plan)
+    h = lib.load()
+    handle = ctypes.c_void_p()
+    crop = (plan.crop_r[0], plan.crop_u[0], plan.nr, plan.nu)
+    assert h.sarbp_ffbp_plan_create(arr, len(arr), *crop, lib.mode_id(mode), ctypes.byref(handle)) == 0
+    # one launch for all leaves + one per tree height (8 merge levels for 256 leaves)
+    assert h.sarbp_ffbp_launch_count(handle) == 9
+    ws = h.sarbp_ffbp_workspace_bytes(handle)
+    images = sum(n.nr * n.nu * 8 for n in plan.nodes()[1:])
+    assert images <= ws <= images * 1.01 + (1 << 26)
+    # binding without a workspace is refused on the host
+    assert h.sarbp_ffbp_bind(handle, None, 0, None) == lib.SARBP_ERR_WORKSPACE
+    h.sarbp_ffbp_plan_destroy(handle)
+    bad = _node_array(lib, plan)
+    bad[0].left = 0  # a child must follow its parent
+    assert h.sarbp_ffbp_plan_create(bad, len(bad), *crop, 3, ctypes.byref(handle)) == lib.SARBP_ERR_PLAN
+
+
+@pytest.mark.parametrize("name", ["c0", "c1", "c3", "validate", "left"])
+def test_product_planner_matches_reference_bit_for_bit(golden, name):
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    g = golden("plans")
+    fc, rmin, rmax, umin, umax, side, leaf, rs, osr = g[f"{name}_args"]
+    plan = build_ffbp_plan(g[f"{name}_position"], fc, (rmin, rmax, umin, umax), side=int(side), leaf_size=int(leaf),
+                           range_spacing=rs, angular_oversample=osr)
+    nodes = plan.nodes()
+    geom = np.array([[*n.origin, n.r0, n.dr, n.u0, n.du, n.side] for n in nodes])
+    idx = np.array([[n.a, n.b, n.nr, n.nu, -1 if n.left is None else n.left.index,
+                     -1 if n.right is None else n.right.index] for n in nodes])
+    np.testing.assert_array_equal(idx, g[f"{name}_idx"])
+    np.testing.assert_array_equal(geom, g[f"{name}_geom"])  # same numpy operations -> identical bits
+    np.testing.assert_array_equal([*plan.crop_r, *plan.crop_u], g[f"{name}_crop"])
+    c = plan.counts
+    np.testing.assert_array_equal([c["leaves"], c["merges"], c["leaf_pixel_pulse_products"], c["merged_pixels"],
+                                   c["nodes"]], g[f"{name}_counts"])
+    np.testing.assert_array_equal([plan.r0, plan.dr, plan.u0, plan.du, plan.nr, plan.nu], g[f"{name}_root"])
+
+
+def test_planner_rejects_disjoint_extent():
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    pos = np.column_stack([np.zeros(32), np.linspace(-5, 5, 32), np.full(32, 100.0)])
+    with pytest.raises(ValueError, match="does not intersect"):
+        build_ffbp_plan(pos, 1e9, (1000.0, 1000.0 + 1e-9, 0.2, 0.2 + 1e-12), leaf_size=8)
+
+
+def test_scene_generation_is_seeded():
+    from bp_project_gb300 import scenes
+    cfg = scenes.scaled(scenes.CONFIGS["c0"], pulses=64, samples=512, image_side=32)
+    a = scenes.synthesize(cfg)
+    b = scenes.synthesize(cfg)
+    assert a.data.dtype == np.complex64 and a.data.shape == (64, 512)
+    np.testing.assert_array_equal(a.data, b.data)
+    assert np.abs(a.data).max() > 0.5  # the targets are in the range window
+    assert a.lattice.points().shape == (32 * 32, 3)
+    rmin, rmax, umin, umax = a.extent
+    assert rmin < cfg.near_slant + 1 and rmax > rmin and umin < 0 < umax
