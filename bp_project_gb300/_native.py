@@ -67,6 +67,9 @@ SIGNATURES = {
     "sarbp_direct_polar_workspace": ([_I, ctypes.POINTER(PolarGrid), _I, _I], _Z),
     "sarbp_direct_polar": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _I, _I, _I, _P, _P, _Z,
                             _P], _I),
+    "sarbp_static_scratch_elements": ([], _Z),
+    "sarbp_direct_polar_static": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _I, _I, _P, _P],
+                                  _I),
     "sarbp_backproject_points_workspace": ([_I, _I, _I], _Z),
     "sarbp_backproject_points": ([_P, _I, _I, _P, _P, _P, _P, _I, _D, _D, _D, _I, _I, _P, _P, _Z, _P], _I),
     "sarbp_backproject_lattice_workspace": ([_I, ctypes.POINTER(Lattice), _I], _Z),

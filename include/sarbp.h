@@ -126,6 +126,26 @@ int sarbp_direct_polar(const float* data, int pulses, int samples, const double*
                        int pulse_split, float* out, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* Allocation-free split-precision direct BP onto a polar grid: the same
+ * result as sarbp_direct_polar(mode = SARBP_SPLIT, same pulse_split), with the
+ * pulse-split partial images held in a fixed device array inside the library
+ * instead of a caller workspace.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory where they image (hosts
+ * that own all device memory through their own pool, real-time loops where
+ * cudaMalloc would synchronise, cgo/JNI hosts that only see the buffers they
+ * were handed).  Limit: pulse_split * nr * nu <= sarbp_static_scratch_elements()
+ * (2^21 complex64, 16 MiB, held by every GPU that loads the library until
+ * exit); larger requests fail with SARBP_ERR_VALUE.  The first call on a device
+ * looks up the array's device address and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Nothing in the array needs clearing: each call overwrites what it reads. */
+size_t sarbp_static_scratch_elements(void);
+int sarbp_direct_polar_static(const float* data, int pulses, int samples, const double* pos,
+                              const double* weight, const double* phase, const sarbp_polar_grid* grid,
+                              double range_start, double data_dr, double k, int chunk_pulses, int pulse_split,
+                              float* out, void* stream);
+
 /* Direct BP at arbitrary points xyz float64 [npts, 3]; out complex64 [npts].
  * Replaces ffbp.backproject_points (fast_bp/ffbp.py:43-55): phase k*r + phase[n],
  * not demodulated.  SPLIT mode groups consecutive points into tiles of 1024;
