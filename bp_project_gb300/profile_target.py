@@ -1,0 +1,83 @@
+"""Nsight / ncu profiling target (counterpart of fast_bp/resident_profile_target.py).
+
+Runs one named workload a few times on cuda:0 so that a profiler can capture
+its kernels:
+
+    python -m bp_project_gb300.profile_target --workload direct --config c1 --reps 2
+    python -m bp_project_gb300.profile_target --workload ffbp   --config c1 --reps 2
+
+Workloads: ``direct`` (split-precision direct BP on the scene's ground
+lattice), ``ffbp`` (level-batched FFBP + evaluate_image onto the lattice),
+``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice).
+Prints one JSON line with event timings (not for benchmarking under a
+profiler: bench.py is the benchmark).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+from . import build, core, scenes
+from .gpu_backend import build_ffbp_plan
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", choices=("direct", "ffbp", "plain"), default="direct")
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--pulses", type=int, default=None, help="scale the scene to this many pulses")
+    ap.add_argument("--side", type=int, default=None, help="scale the ground image to side x side pixels")
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--mode", default="split")
+    args = ap.parse_args(argv)
+    build.build()
+    torch.cuda.set_device(0)
+    cfg = scenes.CONFIGS[args.config]
+    if args.pulses or args.side:
+        cfg = scenes.scaled(cfg, pulses=args.pulses, image_side=args.side)
+    scene = scenes.synthesize(cfg, device="cuda")
+    dev = torch.device("cuda", 0)
+    data = torch.from_numpy(scene.data).to(dev)
+    pos = torch.from_numpy(scene.position).to(dev)
+    wt = torch.from_numpy(scene.weight).to(dev)
+    ph = torch.from_numpy(scene.phase).to(dev)
+    lat = scene.lattice
+    torch.cuda.synchronize()
+    times = []
+    if args.workload in ("direct", "plain"):
+        rows = lat.rows if args.workload == "direct" else 64
+        out = torch.empty((rows, lat.cols), dtype=torch.complex64, device=dev)
+        mode = args.mode if args.workload == "direct" else "mixed"
+
+        def run():
+            core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, rows, lat.cols,
+                                     scene.range_start, scene.data_dr, scene.k, mode=mode, out=out)
+        units = rows * lat.cols * cfg.pulses
+    else:
+        plan = build_ffbp_plan(scene.position, cfg.fc, scene.extent, side=1, leaf_size=cfg.leaf_size,
+                               range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+        prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode=args.mode, device=dev)
+        pts = torch.from_numpy(lat.points()).to(dev)
+        ground = torch.empty(lat.rows * lat.cols, dtype=torch.complex64, device=dev)
+        grid = plan.grid()
+
+        def run():
+            polar = prog.execute(data, pos, wt, ph, scene.range_start, scene.data_dr, scene.k)
+            core.evaluate_image(polar, grid, pts, scene.k, out=ground)
+        units = lat.rows * lat.cols * cfg.pulses
+    for _ in range(args.reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        run()
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    print(json.dumps({"workload": args.workload, "config": cfg.name, "pulses": cfg.pulses,
+                      "image": [lat.rows, lat.cols], "mode": args.mode, "ms": times,
+                      "gpix_pulse_per_s": [units / (t / 1e3) / 1e9 for t in times]}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
