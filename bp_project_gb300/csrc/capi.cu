@@ -137,7 +137,10 @@ struct sarbp_ffbp_plan {
     std::vector<int2> blocks;
     std::vector<int> stage_begin, stage_count;
     int leaf_chunk = 1, leaf_wb = 4;
-    size_t node_bytes = 0, work_bytes = 0, arena_offset = 0, arena_bytes = 0, total_bytes = 0;
+    long long table_entries = 0;  // split: float4 row/column geometry entries of all nodes
+    int max_dim = 1;
+    size_t node_bytes = 0, work_bytes = 0, table_bytes = 0, table_offset = 0, arena_offset = 0, arena_bytes = 0,
+           total_bytes = 0;
     void* bound = nullptr;
     size_t bound_bytes = 0;
     int launches = 0;
@@ -398,6 +401,10 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
             d.out_stride = d.nu;
             arena += align_up((size_t)d.nr * d.nu * sizeof(float2));
         }
+        d.rows_off = p->table_entries;
+        d.cols_off = p->table_entries + d.nr;
+        p->table_entries += (long long)d.nr + d.nu;
+        p->max_dim = std::max(p->max_dim, std::max(d.nr, d.nu));
         double radius = 0.0;
         d.tile_lc = split_polar_tile_lc(d, &radius);
         if (d.left < 0) {
@@ -432,10 +439,12 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
     p->leaf_chunk = leaf_pulses;
     p->node_bytes = align_up(sizeof(PolarDesc) * n_nodes);
     p->work_bytes = align_up(mode == SARBP_SPLIT ? sizeof(TileItem) * p->items.size() : sizeof(int2) * p->blocks.size());
-    p->arena_offset = p->node_bytes + p->work_bytes;
+    p->table_offset = p->node_bytes + p->work_bytes;
+    p->table_bytes = mode == SARBP_SPLIT ? align_up(sizeof(float4) * (size_t)p->table_entries) : 0;
+    p->arena_offset = p->table_offset + p->table_bytes;
     p->arena_bytes = arena;
     p->total_bytes = p->arena_offset + arena;
-    p->launches = p->max_height + 1;
+    p->launches = p->max_height + 1 + (mode == SARBP_SPLIT ? 1 : 0);
     *plan_out = p;
     return SARBP_OK;
 }
@@ -499,10 +508,13 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
             }
         const int wb = split_window_bins(rad, data_dr);
         const int ch = split_chunk_for(wb, plan->leaf_chunk);
-        st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb, arena,
-                                      root_out, 0, s);
+        float4* tables = reinterpret_cast<float4*>(base + plan->table_offset);
+        st = launch_split_ffbp_tables(k, nodes, plan->n_nodes, plan->max_dim, tables, s);
+        if (st == SARBP_OK)
+            st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb,
+                                          tables, arena, root_out, 0, s);
         for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h)
-            st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], arena,
+            st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables, arena,
                                           root_out, 0, s);
     } else {
         const int2* blocks = reinterpret_cast<const int2*>(base + plan->node_bytes);

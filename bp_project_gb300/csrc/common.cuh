@@ -93,6 +93,8 @@ struct PolarDesc {
     long long out_stride;                // row stride (elements) of the output image
     int tile_lc;                         // split kernels: log2 of tile columns (2..5); tile rows = 1024 >> tile_lc
     int pad;
+    long long rows_off;                  // FFBP: first entry of this node's row table (float4 (g_hi, g_lo, psi, 0))
+    long long cols_off;                  // FFBP: first entry of this node's column table (float4 (c_hi, c_lo, u_hi, u_lo))
 };
 
 struct TileItem {
@@ -156,9 +158,13 @@ int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pu
                          int window_bins, float2* out, long long split_stride, cudaStream_t s);
 int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
                         int window_bins, float2* out, long long split_stride, cudaStream_t s);
+// Per-node row/column geometry tables for the FFBP split kernels (one launch per execute).
+int launch_split_ffbp_tables(double k, const PolarDesc* nodes, int n_nodes, int max_dim, float4* tables,
+                             cudaStream_t s);
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             int chunk, int window_bins, float2* arena, float2* root_out, int root, cudaStream_t s);
-int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems, float2* arena,
-                             float2* root_out, int root, cudaStream_t s);
+                             int chunk, int window_bins, const float4* tables, float2* arena, float2* root_out,
+                             int root, cudaStream_t s);
+int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
+                             const float4* tables, float2* arena, float2* root_out, int root, cudaStream_t s);
 
 }  // namespace sarbp

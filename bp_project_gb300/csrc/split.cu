@@ -36,16 +36,18 @@ constexpr int kThreads = kSplitThreads;
 constexpr int kPX = 4;
 constexpr int kMaxRows = kSplitTilePixels >> 2;  // tile_lc >= 2
 constexpr int kMaxCols = 32;                     // tile_lc <= 5
-constexpr int kMaxChunk = 64;
+constexpr int kMaxChunk = 32;                    // one warp computes a chunk's records
 constexpr int kWindowBudget = 96 * 1024;
-
-enum { kPolar = 0, kLattice = 1, kPoints = 2 };
+// K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
+// error, FFBP leaves 1e-4.
+constexpr double kDirectEnvelope = 8.0;
+constexpr double kLeafEnvelope = 64.0;
 
 struct Rec {
     float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y
     float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2
-    float4 c;  // Phi, window bias bits, W_hi.z, W_lo.z
-    float4 d;  // u.z
+    float4 c;  // Phi, window bias bits, window offset bits, window count - 1 bits
+    float4 d;  // u.z, W_hi.z, W_lo.z
 };
 
 struct Pix {
@@ -58,12 +60,14 @@ struct Pix {
 
 struct TileShared {
     double cx, cy, cz;
-    double rho;
+    double rho;                 // bound on |delta_p| (m)
     double scale_d, inv_scale_d;
     double sum[4];
+    float bnd[3];               // bounds on |delta_x|, |delta_y|, |delta_z| (m)
     float red[8][8];
-    int base[kMaxChunk];
+    int base[kMaxChunk];        // global bin of window entry 0, per pulse of the chunk
     float wt[kMaxChunk];
+    int nfit;
 };
 
 // Row/column tables of a polar tile; aliased onto the window region during set-up.
@@ -78,13 +82,17 @@ struct SplitParams {
     PulseInputs in;
     float2* out;           // direct jobs: output image (pulse split s writes out + s * split_stride)
     long long out_stride;
-    double K;          // k / 2pi (turns per metre)
-    double inv_dr;     // 1 / data_dr
+    double K;              // k / 2pi (turns per metre)
+    double inv_dr;         // 1 / data_dr
     double scale_w, inv_scale_w;
     float Kf, inv_drf;
-    int chunk, wb;
+    int chunk;             // pulses per chunk (<= kMaxChunk)
+    int cap;               // window entries (32 bytes each) available per chunk
     int pulse_split;
     long long split_stride;
+    // Precision envelope of the FP32 eps term: the fast path needs K rho^2 / R <= envelope
+    // (the FP32 error of eps is ~2.5e-7 * rho^2 / R metres, i.e. ~2.5e-7 * envelope turns).
+    double envelope;
 };
 
 struct Job {
@@ -94,8 +102,6 @@ struct Job {
     int npts;
     int tile_r, tile_u, lc;
     int p0, p1;
-    float2* out;
-    long long out_stride;
 };
 
 // ---- block reductions (256 threads) ---------------------------------------------
@@ -216,6 +222,9 @@ __device__ void setup_polar(const SplitParams& P, const Job& J, TileShared& S, P
         S.cy = g.oy + gc * uc;
         S.cz = 0.0;
         S.rho = sqrt((double)bx * bx + (double)by * by);
+        S.bnd[0] = bx;
+        S.bnd[1] = by;
+        S.bnd[2] = 0.0f;
         set_quantum(S, fmaxf(bx, by), 12);
     }
     __syncthreads();
@@ -247,6 +256,123 @@ __device__ void setup_polar(const SplitParams& P, const Job& J, TileShared& S, P
     __syncthreads();  // the tables alias the window region
 }
 
+// Polar tile set-up from per-node FP64 tables stored as float pairs (FFBP):
+// FP32 two-float arithmetic only, no block reductions.  Row i holds
+// (g_i hi, g_i lo, psi_i) with g = sqrt(r^2 - oz^2) and psi = frac(-K r);
+// column j holds (c_j hi, c_j lo, u_j hi, u_j lo) with c = sqrt(1 - u^2).
+struct TabF {
+    float rxh[kMaxRows], rxl[kMaxRows], ryh[kMaxRows], ryl[kMaxRows], dg[kMaxRows], psi[kMaxRows];
+    float cxh[kMaxCols], cxl[kMaxCols], cyh[kMaxCols], cyl[kMaxCols], dcs[kMaxCols], duu[kMaxCols];
+};
+
+// (ah + al) * (bh + bl) as an unevaluated pair p + e.
+__device__ __forceinline__ void two_prod(float ah, float al, float bh, float bl, float& p, float& e) {
+    p = ah * bh;
+    e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+}
+
+__device__ __forceinline__ void quantize_pair(float& p, float& e, float q, float iq) {
+    const float h = rintf(p * iq) * q;  // exact: q is a power of two and |p / q| < 2^14
+    e = (p - h) + e;                    // p - h is exact
+    p = h;
+}
+
+__device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const float4* __restrict__ tables,
+                                Pix px[kPX]) {
+    const PolarDesc& g = J.g;
+    const int tid = threadIdx.x;
+    const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
+    const int i0 = min(g.win_r0 + J.tile_r + (rows_t >> 1), g.nr - 1);
+    const int j0 = min(g.win_u0 + J.tile_u + (cols_t >> 1), g.nu - 1);
+    const float4 r0v = __ldg(tables + g.rows_off + i0);
+    const float4 c0v = __ldg(tables + g.cols_off + j0);
+    const float side = (float)g.side;
+    if (tid < rows_t) {
+        const int i = min(g.win_r0 + J.tile_r + tid, g.nr - 1);
+        const float4 rv = __ldg(tables + g.rows_off + i);
+        const float dh = rv.x - r0v.x, dl = rv.y - r0v.y;  // g values of one node: dh is exact
+        float p, e;
+        two_prod(dh, dl, c0v.x, c0v.y, p, e);
+        T.rxh[tid] = side * p;
+        T.rxl[tid] = side * e;
+        two_prod(dh, dl, c0v.z, c0v.w, p, e);
+        T.ryh[tid] = p;
+        T.ryl[tid] = e;
+        T.dg[tid] = dh + dl;
+        T.psi[tid] = rv.z;
+    }
+    if (tid < cols_t) {
+        const int j = min(g.win_u0 + J.tile_u + tid, g.nu - 1);
+        const float4 cv = __ldg(tables + g.cols_off + j);
+        const float ch = cv.x - c0v.x, cl = cv.y - c0v.y;  // c in (0, 1] within a factor 2: exact
+        // u_j - u_0 = (j - j0) du, formed from the integer offset (no cancellation).
+        const float kj = (float)(j - j0);
+        const float duh = (float)g.du, dul = (float)(g.du - (double)duh);
+        const float uh = kj * duh;
+        const float ul = fmaf(kj, duh, -uh) + kj * dul;
+        float p, e;
+        two_prod(r0v.x, r0v.y, ch, cl, p, e);
+        T.cxh[tid] = side * p;
+        T.cxl[tid] = side * e;
+        two_prod(r0v.x, r0v.y, uh, ul, p, e);
+        T.cyh[tid] = p;
+        T.cyl[tid] = e;
+        T.dcs[tid] = side * (ch + cl);
+        T.duu[tid] = uh + ul;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // Row terms are monotone in i and column terms extreme at the tile edges.
+        const int rl = rows_t - 1, cl = cols_t - 1;
+        const float mrx = fmaxf(fabsf(T.rxh[0]), fabsf(T.rxh[rl])), mry = fmaxf(fabsf(T.ryh[0]), fabsf(T.ryh[rl]));
+        const float mdg = fmaxf(fabsf(T.dg[0]), fabsf(T.dg[rl]));
+        const float mcx = fmaxf(fabsf(T.cxh[0]), fabsf(T.cxh[cl])), mcy = fmaxf(fabsf(T.cyh[0]), fabsf(T.cyh[cl]));
+        const float mdc = fmaxf(fabsf(T.dcs[0]), fabsf(T.dcs[cl])), mdu = fmaxf(fabsf(T.duu[0]), fabsf(T.duu[cl]));
+        const float bx = (mrx + mcx + mdg * mdc) * 1.0001f + 1e-6f;
+        const float by = (mry + mcy + mdg * mdu) * 1.0001f + 1e-6f;
+        S.bnd[0] = bx;
+        S.bnd[1] = by;
+        S.bnd[2] = 0.0f;
+        S.rho = sqrt((double)bx * bx + (double)by * by);
+        set_quantum(S, fmaxf(bx, by), 12);
+        const double g0 = (double)r0v.x + (double)r0v.y;
+        const double c0 = (double)c0v.x + (double)c0v.y, u0 = (double)c0v.z + (double)c0v.w;
+        S.cx = g.ox + (double)g.side * g0 * c0;
+        S.cy = g.oy + g0 * u0;
+        S.cz = 0.0;
+    }
+    __syncthreads();
+    const float q = (float)S.scale_d, iq = (float)S.inv_scale_d;
+    if (tid < rows_t) {
+        quantize_pair(T.rxh[tid], T.rxl[tid], q, iq);
+        quantize_pair(T.ryh[tid], T.ryl[tid], q, iq);
+    }
+    if (tid < cols_t) {
+        quantize_pair(T.cxh[tid], T.cxl[tid], q, iq);
+        quantize_pair(T.cyh[tid], T.cyl[tid], q, iq);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = tid + kThreads * k;
+        const int row = p >> J.lc, col = p & (cols_t - 1);
+        Pix& v = px[k];
+        v.dxh = T.rxh[row] + T.cxh[col];
+        v.dyh = T.ryh[row] + T.cyh[col];
+        v.dxl = fmaf(T.dg[row], T.dcs[col], T.rxl[row] + T.cxl[col]);
+        v.dyl = fmaf(T.dg[row], T.duu[col], T.ryl[row] + T.cyl[col]);
+        v.dzh = v.dzl = v.dz = 0.0f;
+        v.dx = v.dxh + v.dxl;
+        v.dy = v.dyh + v.dyl;
+        v.d2 = v.dx * v.dx + v.dy * v.dy;
+        v.psi = T.psi[row];
+        v.ar = v.ai = 0.0f;
+    }
+    __syncthreads();  // the tables alias the window region
+}
+
 template <bool HAS_Z>
 __device__ void setup_lattice(const Job& J, TileShared& S, Pix px[kPX]) {
     const sarbp_lattice& L = J.lat;
@@ -261,6 +387,7 @@ __device__ void setup_lattice(const Job& J, TileShared& S, Pix px[kPX]) {
         double b[3];
         for (int c = 0; c < 3; ++c) b[c] = hr * fabs(L.step_row[c]) + hc * fabs(L.step_col[c]);
         S.rho = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) * 1.0001 + 1e-6;
+        for (int c = 0; c < 3; ++c) S.bnd[c] = (float)(b[c] * 1.0001 + 1e-6);
         set_quantum(S, (float)(fmax(b[0], fmax(b[1], b[2])) * 1.0001 + 1e-6), HAS_Z ? 11 : 12);
     }
     __syncthreads();
@@ -311,6 +438,9 @@ __device__ void setup_points(const Job& J, TileShared& S, Pix px[kPX]) {
         S.cz = cz;
         const double b0 = m[0] * 1.0001 + 1e-6, b1 = m[1] * 1.0001 + 1e-6, b2 = m[2] * 1.0001 + 1e-6;
         S.rho = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+        S.bnd[0] = (float)b0;
+        S.bnd[1] = (float)b1;
+        S.bnd[2] = (float)b2;
         set_quantum(S, (float)fmax(b0, fmax(b1, b2)), 11);
     }
     __syncthreads();
@@ -324,23 +454,23 @@ __device__ void setup_points(const Job& J, TileShared& S, Pix px[kPX]) {
 }
 
 // ---- the pulse loop ---------------------------------------------------------------
-template <bool HAS_Z>
+template <bool HAS_Z, bool DEMOD>
 __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __restrict__ rec,
                                            const float4* __restrict__ win, int chn, Pix px[kPX]) {
-    const unsigned wbm1 = (unsigned)(P.wb - 1);
     const float inv_dr = P.inv_drf, Kf = P.Kf;
 #pragma unroll 1
     for (int nl = 0; nl < chn; ++nl) {
         const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c;
-        float uz = 0.0f;
-        if (HAS_Z) uz = rec[nl].d.x;
-        const int cb = __float_as_int(rc.y);
-        const float4* wrow = win + (size_t)nl * P.wb * 2;
+        float4 rd = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (HAS_Z) rd = rec[nl].d;
+        const int bias = __float_as_int(rc.y);
+        const unsigned last = (unsigned)__float_as_int(rc.w);
+        const float4* wrow = win + 2 * __float_as_int(rc.z);
 #pragma unroll
         for (int k = 0; k < kPX; ++k) {
             Pix& q = px[k];
             float L = fmaf(rb.x, q.dx, rb.y * q.dy);
-            if (HAS_Z) L = fmaf(uz, q.dz, L);
+            if (HAS_Z) L = fmaf(rd.x, q.dz, L);
             const float q2 = fmaf(-L, L, q.d2);
             const float B = rcp_approx(fmaf(2.0f, L, rb.z));
             const float e0 = q2 * B;
@@ -348,24 +478,24 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
             const float qp = fmaf(L + eps, inv_dr, rb.w);
             const float tq = qp + kMagic;
             const float s = qp - (tq - kMagic);
-            const unsigned j = min((unsigned)(__float_as_int(tq) - cb), wbm1);
+            const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
             const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
             const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
             const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
             float tb = ra.y * q.dyh;
-            if (HAS_Z) tb = fmaf(rc.z, q.dzh, tb);
+            if (HAS_Z) tb = fmaf(rd.y, q.dzh, tb);
             tb = fmaf(ra.x, q.dxh, tb);
-            const float fb = tb - round_magic(tb);
             float sm = fmaf(Kf, eps, rc.x);
             sm = fmaf(ra.x, q.dxl, sm);
             sm = fmaf(ra.y, q.dyl, sm);
             sm = fmaf(ra.z, q.dx, sm);
             sm = fmaf(ra.w, q.dy, sm);
             if (HAS_Z) {
-                sm = fmaf(rc.z, q.dzl, sm);
-                sm = fmaf(rc.w, q.dz, sm);
+                sm = fmaf(rd.y, q.dzl, sm);
+                sm = fmaf(rd.z, q.dz, sm);
             }
-            const float tot = (fb + q.psi) + sm;
+            if (DEMOD) sm += q.psi;
+            const float tot = (tb - round_magic(tb)) + sm;
             const float ang = (tot - round_magic(tot)) * kTwoPiF;
             float sn, cs;
             __sincosf(ang, &sn, &cs);
@@ -377,112 +507,140 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
     }
 }
 
-// FP64 per-sample fallback for chunks whose windows do not fit (very large tiles).
-__device__ __forceinline__ void slow_chunk(const SplitParams& P, const TileShared& S, int c0, int chn, Pix px[kPX]) {
-    const PulseInputs& in = P.in;
-    for (int nl = 0; nl < chn; ++nl) {
-        const int n = c0 + nl;
-        const double pxn = in.pos[3 * n], pyn = in.pos[3 * n + 1], pzn = in.pos[3 * n + 2];
-        const double ph = in.phase[n] * kInvTwoPi;
-        const float a = (float)in.weight[n];
-        const float2* row = in.data + (size_t)n * in.samples;
-        for (int k = 0; k < kPX; ++k) {
-            Pix& q = px[k];
-            const double x = S.cx + ((double)q.dxh + (double)q.dxl) - pxn;
-            const double y = S.cy + ((double)q.dyh + (double)q.dyl) - pyn;
-            const double z = S.cz + ((double)q.dzh + (double)q.dzl) - pzn;
-            const double d = sqrt(x * x + y * y + z * z);
-            const double t = P.K * d + ph;
-            const float tot = (float)(t - rint(t)) + q.psi;
-            const float ang = (tot - round_magic(tot)) * kTwoPiF;
-            const double qq = (d - in.range_start) * P.inv_dr;
-            const double fl = floor(qq);
-            if (!(fl >= 1.0 && fl <= (double)(in.samples - 3))) continue;
-            const int i = (int)fl;
-            float w[4];
-            lagrange_centred((float)(qq - fl - 0.5), w);
-            float vr = 0.0f, vi = 0.0f;
+// FP64 per-sample evaluation of one pixel over pulses [c0, c0 + chn): the
+// fallback for a pulse whose range window does not fit the staged bins.
+// Everything is passed by value so the caller's pixel state stays in registers.
+__device__ __noinline__ float2 slow_pixel(const float2* __restrict__ data, int samples, const double* __restrict__ pos,
+                                          const double* __restrict__ weight, const double* __restrict__ phase,
+                                          double range_start, double inv_dr, double K, double x, double y, double z,
+                                          float psi, int c0, int chn) {
+    float ar = 0.0f, ai = 0.0f;
+    for (int n = c0; n < c0 + chn; ++n) {
+        const double vx = x - pos[3 * n], vy = y - pos[3 * n + 1], vz = z - pos[3 * n + 2];
+        const double d = sqrt(vx * vx + vy * vy + vz * vz);
+        const double t = K * d + phase[n] * kInvTwoPi;
+        const float tot = (float)(t - rint(t)) + psi;
+        const float ang = (tot - round_magic(tot)) * kTwoPiF;
+        const double qq = (d - range_start) * inv_dr;
+        const double fl = floor(qq);
+        if (!(fl >= 1.0 && fl <= (double)(samples - 3))) continue;
+        const int i = (int)fl;
+        const float2* row = data + (size_t)n * samples;
+        float w[4];
+        lagrange_centred((float)(qq - fl - 0.5), w);
+        float vr = 0.0f, vi = 0.0f;
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const float2 v = __ldg(row + i + b - 1);
-                vr = fmaf(w[b], v.x, vr);
-                vi = fmaf(w[b], v.y, vi);
-            }
-            vr *= a;
-            vi *= a;
-            float sn, cs;
-            __sincosf(ang, &sn, &cs);
-            q.ar = fmaf(vr, cs, q.ar);
-            q.ar = fmaf(-vi, sn, q.ar);
-            q.ai = fmaf(vr, sn, q.ai);
-            q.ai = fmaf(vi, cs, q.ai);
+        for (int b = 0; b < 4; ++b) {
+            const float2 v = __ldg(row + i + b - 1);
+            vr = fmaf(w[b], v.x, vr);
+            vi = fmaf(w[b], v.y, vi);
         }
+        const float a = (float)weight[n];
+        float sn, cs;
+        __sincosf(ang, &sn, &cs);
+        ar = fmaf(a * vr, cs, fmaf(-a * vi, sn, ar));
+        ai = fmaf(a * vr, sn, fmaf(a * vi, cs, ai));
     }
+    return make_float2(ar, ai);
 }
 
-template <bool HAS_Z>
+// Per (tile, pulse) record in FP64, computed by lane `lane` of warp 0.  Returns
+// the number of window entries the pulse needs (cap + 1 if it cannot be staged).
+__device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, Rec* rec, int lane, int n) {
+    const PulseInputs& in = P.in;
+    const double vx = S.cx - in.pos[3 * n], vy = S.cy - in.pos[3 * n + 1], vz = S.cz - in.pos[3 * n + 2];
+    const double R = sqrt(vx * vx + vy * vy + vz * vz);
+    const double iR = 1.0 / R;
+    const double ux = vx * iR, uy = vy * iR, uz = vz * iR;
+    const double t1 = P.K * R + in.phase[n] * kInvTwoPi;
+    const double Q = (R - in.range_start) * P.inv_dr;
+    const double I = floor(Q);
+    const double Fm = (Q - I) - 0.5;
+    // |L| <= sum_c |u_c| bound_c and 0 <= eps <= rho^2 / (2 (R - rho)), in bins.
+    const double lin = fabs(ux) * S.bnd[0] + fabs(uy) * S.bnd[1] + fabs(uz) * S.bnd[2];
+    const double eps = S.rho * S.rho / (2.0 * fmax(R - S.rho, 1.0));
+    const double hw = (lin + eps) * fabs(P.inv_dr) + 1e-3;
+    const double lo = floor(Fm - hw), hi = ceil(Fm + hw);
+    const bool ok = R > 0.0 && fabs(Q) < 1.0e9 && hi - lo + 1.0 <= (double)P.cap &&
+                    fabs(P.K) * S.rho * S.rho <= P.envelope * R && S.rho < 0.25 * R;
+    const int bo = ok ? (int)lo : 0;
+    S.base[lane] = ok ? (int)I + bo : 0;
+    S.wt[lane] = (float)in.weight[n];
+    Rec r;
+    quantize(P.K * ux, P.scale_w, P.inv_scale_w, r.a.x, r.a.z);
+    quantize(P.K * uy, P.scale_w, P.inv_scale_w, r.a.y, r.a.w);
+    quantize(P.K * uz, P.scale_w, P.inv_scale_w, r.d.y, r.d.z);
+    r.b = make_float4((float)ux, (float)uy, (float)(2.0 * R), (float)Fm);
+    r.c.x = (float)(t1 - rint(t1));
+    r.c.y = __int_as_float(kMagicBits + bo);
+    r.d.x = (float)uz;
+    r.d.w = 0.0f;
+    const int count = ok ? (int)(hi - lo) + 1 : P.cap + 1;
+    r.c.z = 0.0f;
+    r.c.w = __int_as_float(count - 1);
+    rec[lane] = r;
+    return count;
+}
+
+template <bool HAS_Z, bool DEMOD>
 __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, Pix px[kPX]) {
     const PulseInputs& in = P.in;
-    const int tid = threadIdx.x;
-    const int CH = P.chunk, WB = P.wb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Rec* rec = reinterpret_cast<Rec*>(smem);
-    float4* win = reinterpret_cast<float4*>(smem + (size_t)CH * sizeof(Rec));
-    for (int c0 = J.p0; c0 < J.p1; c0 += CH) {
-        const int chn = min(CH, J.p1 - c0);
-        __syncthreads();
-        int bad = 0;
-        if (tid < chn) {
-            const int n = c0 + tid;
-            const double vx = S.cx - in.pos[3 * n], vy = S.cy - in.pos[3 * n + 1], vz = S.cz - in.pos[3 * n + 2];
-            const double R = sqrt(vx * vx + vy * vy + vz * vz);
-            const double iR = 1.0 / R;
-            const double ux = vx * iR, uy = vy * iR, uz = vz * iR;
-            const double t1 = P.K * R + in.phase[n] * kInvTwoPi;
-            const double Q = (R - in.range_start) * P.inv_dr;
-            const double I = floor(Q);
-            const double Fm = (Q - I) - 0.5;
-            const double wing = (S.rho + S.rho * S.rho * iR) * fabs(P.inv_dr) + 0.01;
-            const double lo = floor(Fm - wing), hi = ceil(Fm + wing);
-            bad = !(R > 0.0) || !(fabs(Q) < 1.0e9) || !(hi - lo + 1.0 <= (double)WB);
-            const int bo = bad ? 0 : (int)lo;
-            S.base[tid] = bad ? 0 : (int)I + bo;
-            S.wt[tid] = (float)in.weight[n];
-            Rec r;
-            quantize(P.K * ux, P.scale_w, P.inv_scale_w, r.a.x, r.a.z);
-            quantize(P.K * uy, P.scale_w, P.inv_scale_w, r.a.y, r.a.w);
-            quantize(P.K * uz, P.scale_w, P.inv_scale_w, r.c.z, r.c.w);
-            r.b = make_float4((float)ux, (float)uy, (float)(2.0 * R), (float)Fm);
-            r.c.x = (float)(t1 - rint(t1));
-            r.c.y = __int_as_float(kMagicBits + bo);
-            r.d = make_float4((float)uz, 0.0f, 0.0f, 0.0f);
-            rec[tid] = r;
-        }
-        const int slow = __syncthreads_or(bad);
-        if (!slow) {
-            const int total = chn * WB;
-            for (int e = tid; e < total; e += kThreads) {
-                const int nl = e / WB;
-                const int j = e - nl * WB;
-                const long long gbin = (long long)S.base[nl] + j;
-                float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
-                if (gbin >= 1 && gbin <= (long long)in.samples - 3) {
-                    const float2* row = in.data + (size_t)(c0 + nl) * in.samples + gbin;
-                    cubic_coefficients(__ldg(row - 1), __ldg(row), __ldg(row + 1), __ldg(row + 2), S.wt[nl], c01,
-                                       c23);
-                }
-                win[2 * e] = c01;
-                win[2 * e + 1] = c23;
+    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxChunk * sizeof(Rec));
+    for (int c0 = J.p0; c0 < J.p1;) {
+        const int want = min(P.chunk, J.p1 - c0);
+        __syncthreads();  // the previous chunk's records and windows are consumed
+        if (warp == 0) {
+            const int count = lane < want ? make_record(P, S, rec, lane, c0 + lane) : 0;
+            int inc = count;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
             }
+            // Counts are >= 1, so the pulses that fit form a prefix of the chunk.
+            const unsigned fits = __ballot_sync(0xffffffffu, lane < want && inc <= P.cap);
+            if (lane < want) rec[lane].c.z = __int_as_float(inc - count);
+            if (lane == 0) S.nfit = __popc(fits);
         }
         __syncthreads();
-        if (!slow) {
-            fast_chunk<HAS_Z>(P, rec, win, chn, px);
+        const int nfit = S.nfit;
+        if (nfit > 0) {
+            for (int nl = warp; nl < nfit; nl += kThreads / 32) {
+                const int off = __float_as_int(rec[nl].c.z);
+                const int cnt = __float_as_int(rec[nl].c.w) + 1;
+                const long long b0 = S.base[nl];
+                const float a = S.wt[nl];
+                const float2* row = in.data + (size_t)(c0 + nl) * in.samples;
+                for (int j = lane; j < cnt; j += 32) {
+                    const long long g = b0 + j;
+                    float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
+                    if (g >= 1 && g <= (long long)in.samples - 3)
+                        cubic_coefficients(__ldg(row + g - 1), __ldg(row + g), __ldg(row + g + 1), __ldg(row + g + 2),
+                                           a, c01, c23);
+                    win[2 * (off + j)] = c01;
+                    win[2 * (off + j) + 1] = c23;
+                }
+            }
+            __syncthreads();
+            fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px);
+            c0 += nfit;
         } else {
-            slow_chunk(P, S, c0, chn, px);
+#pragma unroll
+            for (int k = 0; k < kPX; ++k) {
+                Pix& q = px[k];
+                const float2 v = slow_pixel(in.data, in.samples, in.pos, in.weight, in.phase, in.range_start, P.inv_dr,
+                                            P.K, S.cx + ((double)q.dxh + (double)q.dxl),
+                                            S.cy + ((double)q.dyh + (double)q.dyl),
+                                            S.cz + ((double)q.dzh + (double)q.dzl), DEMOD ? q.psi : 0.0f, c0, 1);
+                q.ar += v.x;
+                q.ai += v.y;
+            }
+            c0 += 1;
         }
     }
 }
-
 
 // ---- output ----------------------------------------------------------------------
 __device__ __forceinline__ void store_window(const Job& J, int win_nr, int win_nu, const Pix px[kPX], float2* out,
@@ -510,7 +668,7 @@ __device__ __forceinline__ void tile_of(int index, int win_nu, int lc, int& tile
 }
 
 // ---- direct BP kernels --------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 2) split_polar_kernel(SplitParams P, PolarDesc g) {
+__global__ void __launch_bounds__(kThreads, 3) split_polar_kernel(SplitParams P, PolarDesc g) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     Job J;
@@ -519,14 +677,14 @@ __global__ void __launch_bounds__(kThreads, 2) split_polar_kernel(SplitParams P,
     tile_of(blockIdx.x, g.win_nu, J.lc, J.tile_r, J.tile_u);
     split_range(g.a, g.b, P.pulse_split, blockIdx.y, J.p0, J.p1);
     Pix px[kPX];
-    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)P.chunk * sizeof(Rec));
+    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)kMaxChunk * sizeof(Rec));
     setup_polar(P, J, S, T, px, true);
-    pulse_loop<false>(P, J, S, smem, px);
+    pulse_loop<false, true>(P, J, S, smem, px);
     store_window(J, g.win_nr, g.win_nu, px, P.out + blockIdx.y * P.split_stride, P.out_stride);
 }
 
 template <bool HAS_Z>
-__global__ void __launch_bounds__(kThreads, 2) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
+__global__ void __launch_bounds__(kThreads, 3) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     Job J;
@@ -536,11 +694,11 @@ __global__ void __launch_bounds__(kThreads, 2) split_lattice_kernel(SplitParams 
     split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, J.p0, J.p1);
     Pix px[kPX];
     setup_lattice<HAS_Z>(J, S, px);
-    pulse_loop<HAS_Z>(P, J, S, smem, px);
+    pulse_loop<HAS_Z, false>(P, J, S, smem, px);
     store_window(J, lat.rows, lat.cols, px, P.out + blockIdx.y * P.split_stride, lat.cols);
 }
 
-__global__ void __launch_bounds__(kThreads, 2) split_points_kernel(SplitParams P, const double* __restrict__ xyz,
+__global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P, const double* __restrict__ xyz,
                                                                    int npts) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
@@ -553,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, 2) split_points_kernel(SplitParams P
     split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, J.p0, J.p1);
     Pix px[kPX];
     setup_points(J, S, px);
-    pulse_loop<true>(P, J, S, smem, px);
+    pulse_loop<true, false>(P, J, S, smem, px);
     float2* out = P.out + blockIdx.y * P.split_stride;
 #pragma unroll
     for (int k = 0; k < kPX; ++k) {
@@ -563,8 +721,9 @@ __global__ void __launch_bounds__(kThreads, 2) split_points_kernel(SplitParams P
 }
 
 // ---- FFBP: leaves ---------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 2) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                  const TileItem* __restrict__ items,
+                                                                 const float4* __restrict__ tables,
                                                                  float2* __restrict__ arena, float2* root_out,
                                                                  int root) {
     extern __shared__ __align__(16) char smem[];
@@ -578,11 +737,30 @@ __global__ void __launch_bounds__(kThreads, 2) split_leaf_kernel(SplitParams P, 
     J.p0 = J.g.a;
     J.p1 = J.g.b;
     Pix px[kPX];
-    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)P.chunk * sizeof(Rec));
-    setup_polar(P, J, S, T, px, true);
-    pulse_loop<false>(P, J, S, smem, px);
+    TabF& T = *reinterpret_cast<TabF*>(smem + (size_t)kMaxChunk * sizeof(Rec));
+    setup_polar_tab(J, S, T, tables, px);
+    pulse_loop<false, true>(P, J, S, smem, px);
     float2* dst = it.node == root ? root_out : arena + J.g.out_offset;
     store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+}
+
+// Per-node geometry tables (FP64 once per row / column, stored as float pairs).
+__global__ void ffbp_tables_kernel(double K, const PolarDesc* __restrict__ nodes, float4* __restrict__ tables) {
+    const PolarDesc& g = nodes[blockIdx.y];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < g.nr) {
+        const double r = g.r0 + (double)t * g.dr;
+        const double gg = sqrt(fmax(0.0, r * r - g.oz * g.oz));
+        const float gh = (float)gg;
+        const double ph = -K * r;
+        tables[g.rows_off + t] = make_float4(gh, (float)(gg - (double)gh), (float)(ph - rint(ph)), 0.0f);
+    }
+    if (t < g.nu) {
+        const double u = g.u0 + (double)t * g.du;
+        const double c = sqrt(fmax(0.0, 1.0 - u * u));
+        const float chh = (float)c, uh = (float)u;
+        tables[g.cols_off + t] = make_float4(chh, (float)(c - (double)chh), uh, (float)(u - (double)uh));
+    }
 }
 
 // ---- FFBP: merges (both child regrids of one parent tile) --------------------------------
@@ -682,6 +860,7 @@ __device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildR
 
 __global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
+                                                                  const float4* __restrict__ tables,
                                                                   float2* __restrict__ arena, float2* root_out,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
@@ -694,8 +873,8 @@ __global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P,
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
     Pix px[kPX];
-    PolarTables& T = *reinterpret_cast<PolarTables*>(smem);
-    setup_polar(P, J, S, T, px, true);
+    TabF& T = *reinterpret_cast<TabF*>(smem);
+    setup_polar_tab(J, S, T, tables, px);
     if (threadIdx.x < 2) {
         const int child = threadIdx.x == 0 ? J.g.left : J.g.right;
         const PolarDesc c = nodes[child];
@@ -713,7 +892,7 @@ __global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P,
     store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
 }
 
-SplitParams make_params(const PulseInputs& in, int chunk, int wb, int pulse_split) {
+SplitParams make_params(const PulseInputs& in, int chunk, int cap, int pulse_split) {
     SplitParams P;
     P.in = in;
     P.out = nullptr;
@@ -726,17 +905,18 @@ SplitParams make_params(const PulseInputs& in, int chunk, int wb, int pulse_spli
     P.inv_scale_w = ldexp(1.0, 10 - e);
     P.Kf = (float)P.K;
     P.inv_drf = (float)P.inv_dr;
-    P.chunk = chunk;
-    P.wb = wb;
+    P.chunk = chunk < 1 ? 1 : (chunk > kMaxChunk ? kMaxChunk : chunk);
+    P.cap = cap < 4 ? 4 : cap;
     P.pulse_split = pulse_split;
     P.split_stride = 0;
+    P.envelope = kDirectEnvelope;
     return P;
 }
 
-size_t dynamic_smem(int chunk, int wb, bool polar) {
-    size_t win = (size_t)chunk * wb * 32;
+size_t dynamic_smem(int cap, bool polar) {
+    size_t win = (size_t)cap * 32;
     if (polar && win < sizeof(PolarTables)) win = sizeof(PolarTables);
-    return (size_t)chunk * sizeof(Rec) + win;
+    return (size_t)kMaxChunk * sizeof(Rec) + win;
 }
 
 template <class K>
@@ -753,10 +933,20 @@ int tiles_of(int nr, int nu, int lc) {
     return ((nr + rows_t - 1) / rows_t) * ((nu + cols_t - 1) / cols_t);
 }
 
+// Window entries for one chunk: `chunk` pulses whose windows span at most
+// `window_bins` bins each (the kernel packs the actual, usually smaller, windows).
+int capacity_for(int chunk, int window_bins) {
+    long long cap = (long long)chunk * window_bins;
+    const long long budget = kWindowBudget / 32;
+    return (int)(cap > budget ? budget : cap);
+}
+
 }  // namespace
 
 int split_window_bins(double radius, double data_dr) {
-    const double wing = (radius + radius * radius / 100.0) / fabs(data_dr) + 0.01;
+    // Worst case: the pixel offset lies along the line of sight; eps <= radius^2/(2(R - radius)) is
+    // small at any range used here (R >= 100 m gives the bound below).
+    const double wing = (radius + radius * radius / 200.0) / fabs(data_dr) + 0.01;
     return (int)ceil(2.0 * wing) + 4;
 }
 
@@ -793,11 +983,11 @@ int split_polar_tile_lc(const PolarDesc& g, double* radius) {
 
 int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_split, int chunk, int window_bins,
                        float2* out, long long out_stride, long long split_stride, cudaStream_t s) {
-    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), pulse_split);
     P.out = out;
     P.out_stride = out_stride;
     P.split_stride = split_stride;
-    const size_t smem = dynamic_smem(chunk, window_bins, true);
+    const size_t smem = dynamic_smem(P.cap, true);
     if (int st = prepare(split_polar_kernel, smem)) return st;
     dim3 grid(tiles_of(g.win_nr, g.win_nu, g.tile_lc), pulse_split);
     split_polar_kernel<<<grid, kThreads, smem, s>>>(P, g);
@@ -807,11 +997,11 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
 
 int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk, int window_bins,
                          float2* out, long long split_stride, cudaStream_t s) {
-    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), pulse_split);
     P.out = out;
     P.split_stride = split_stride;
     const int lc = 5;
-    const size_t smem = dynamic_smem(chunk, window_bins, false);
+    const size_t smem = dynamic_smem(P.cap, false);
     dim3 grid(tiles_of(lat.rows, lat.cols, lc), pulse_split);
     const bool has_z = lat.step_row[2] != 0.0 || lat.step_col[2] != 0.0;
     if (has_z) {
@@ -827,10 +1017,10 @@ int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pu
 
 int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
                         int window_bins, float2* out, long long split_stride, cudaStream_t s) {
-    SplitParams P = make_params(in, chunk, window_bins, pulse_split);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), pulse_split);
     P.out = out;
     P.split_stride = split_stride;
-    const size_t smem = dynamic_smem(chunk, window_bins, false);
+    const size_t smem = dynamic_smem(P.cap, false);
     if (int st = prepare(split_points_kernel, smem)) return st;
     dim3 grid((npts + kSplitTilePixels - 1) / kSplitTilePixels, pulse_split);
     split_points_kernel<<<grid, kThreads, smem, s>>>(P, xyz, npts);
@@ -838,27 +1028,40 @@ int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int 
     return check_launch("split_points");
 }
 
+int launch_split_ffbp_tables(double k, const PolarDesc* nodes, int n_nodes, int max_dim, float4* tables,
+                             cudaStream_t s) {
+    if (n_nodes <= 0) return SARBP_OK;
+    dim3 grid((max_dim + kThreads - 1) / kThreads, n_nodes);
+    ffbp_tables_kernel<<<grid, kThreads, 0, s>>>(k * kInvTwoPi, nodes, tables);
+    note_launches(1);
+    return check_launch("split_ffbp_tables");
+}
+
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             int chunk, int window_bins, float2* arena, float2* root_out, int root, cudaStream_t s) {
+                             int chunk, int window_bins, const float4* tables, float2* arena, float2* root_out,
+                             int root, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
-    SplitParams P = make_params(in, chunk, window_bins, 1);
-    const size_t smem = dynamic_smem(chunk, window_bins, true);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
+    P.envelope = kLeafEnvelope;
+    size_t smem = dynamic_smem(P.cap, false);
+    const size_t need = (size_t)kMaxChunk * sizeof(Rec) + sizeof(TabF);
+    if (smem < need) smem = need;
     if (int st = prepare(split_leaf_kernel, smem)) return st;
-    split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, arena, root_out, root);
+    split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_leaves");
 }
 
-int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems, float2* arena,
-                             float2* root_out, int root, cudaStream_t s) {
+int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
+                             const float4* tables, float2* arena, float2* root_out, int root, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
     none.data_dr = 1.0;
-    SplitParams P = make_params(none, 0, 0, 1);
-    const size_t smem = sizeof(PolarTables);
+    SplitParams P = make_params(none, 1, 4, 1);
+    const size_t smem = sizeof(TabF);
     if (int st = prepare(split_merge_kernel, smem)) return st;
-    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, arena, root_out, root);
+    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_merges");
 }

@@ -169,6 +169,31 @@ def test_c1_direct_sampled_pixels(lib):
     assert err <= 1e-5
 
 
+@pytest.mark.slow
+def test_c1_ffbp_vs_reference_ffbp(lib):
+    """Config 1 at full size: split FFBP (16-pulse leaves, 8 merge levels, root 3084 x 25031) within 1e-4 of the
+    reference FFBP (oracle restatement of ffbp.form_ffbp on the same plan)."""
+    from bp_project_gb300 import core
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    from oracle import reference as ora
+    sc = _scene("c1")
+    cfg = sc.config
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split")
+    img = prog.execute(_dev(sc.data, torch.complex64), _dev(sc.position, torch.float64),
+                       _dev(sc.weight, torch.float64), _dev(sc.phase, torch.float64), sc.range_start, sc.data_dr,
+                       sc.k).cpu().numpy()
+    prog.close()
+    ref, counts = ora.form_ffbp(sc.data, sc.position, sc.range_start, sc.data_dr, cfg.fc, sc.extent, side=1,
+                                leaf_size=cfg.leaf_size, range_spacing=cfg.range_spacing,
+                                angular_oversample=cfg.angular_oversample, weight=sc.weight, phase=sc.phase)
+    assert counts["leaves"] == 256 and counts["merges"] == 255
+    err = rel_err(ref.image, img)
+    print(f"c1 split FFBP vs reference FFBP: {err:.3e}")
+    assert err <= 1e-4
+
+
 def test_linearity_and_pulse_split(lib):
     """BP is linear in the data; splitting the aperture over CTAs changes only FP32 rounding."""
     from bp_project_gb300 import scenes
