@@ -139,7 +139,12 @@ struct sarbp_ffbp_plan {
     int leaf_chunk = 1, leaf_wb = 4;
     long long table_entries = 0;  // split: float4 row/column geometry entries of all nodes
     int max_dim = 1;
-    size_t node_bytes = 0, work_bytes = 0, table_bytes = 0, table_offset = 0, arena_offset = 0, arena_bytes = 0,
+    std::vector<int> leaves;      // split: leaf node indices
+    int max_pulse = 0;            // split: largest pulse index + 1 used by a leaf
+    int leaf_span_bins = 4;       // split: range bins a 32-row leaf tile spans (before the pulse offsets)
+    long long merge_items = 0;    // split: tile items of all merge levels (contiguous after the leaves)
+    size_t node_bytes = 0, work_bytes = 0, leaf_list_bytes = 0, table_bytes = 0, table_offset = 0,
+           prec_offset = 0, prec_bytes = 0, crec_offset = 0, crec_bytes = 0, arena_offset = 0, arena_bytes = 0,
            total_bytes = 0;
     void* bound = nullptr;
     size_t bound_bytes = 0;
@@ -402,11 +407,18 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
             arena += align_up((size_t)d.nr * d.nu * sizeof(float2));
         }
         d.rows_off = p->table_entries;
-        d.cols_off = p->table_entries + d.nr;
-        p->table_entries += (long long)d.nr + d.nu;
+        d.cols_off = p->table_entries + 3LL * d.nr;
+        p->table_entries += 3LL * d.nr + d.nu;
         p->max_dim = std::max(p->max_dim, std::max(d.nr, d.nu));
         double radius = 0.0;
         d.tile_lc = split_polar_tile_lc(d, &radius);
+        if (d.left < 0 && mode == SARBP_SPLIT) {
+            // Leaves use the origin formulation: precision does not depend on the tile shape, and
+            // 32-row tiles keep each pulse's range window short.
+            d.tile_lc = 5;
+            p->leaves.push_back(i);
+            p->max_pulse = std::max(p->max_pulse, d.b);
+        }
         if (d.left < 0) {
             leaf_radius = std::max(leaf_radius, radius);
             leaf_pulses = std::max(leaf_pulses, d.b - d.a);
@@ -439,12 +451,20 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
     p->leaf_chunk = leaf_pulses;
     p->node_bytes = align_up(sizeof(PolarDesc) * n_nodes);
     p->work_bytes = align_up(mode == SARBP_SPLIT ? sizeof(TileItem) * p->items.size() : sizeof(int2) * p->blocks.size());
-    p->table_offset = p->node_bytes + p->work_bytes;
-    p->table_bytes = mode == SARBP_SPLIT ? align_up(sizeof(float4) * (size_t)p->table_entries) : 0;
-    p->arena_offset = p->table_offset + p->table_bytes;
+    if (mode == SARBP_SPLIT) {
+        p->merge_items = (long long)p->items.size() - p->stage_count[0];
+        p->leaf_list_bytes = align_up(sizeof(int) * p->leaves.size());
+        p->table_bytes = align_up(sizeof(float4) * (size_t)p->table_entries);
+        p->prec_bytes = align_up(split_ffbp_pulse_record_bytes() * (size_t)p->max_pulse);
+        p->crec_bytes = align_up(split_ffbp_child_record_bytes() * 2 * (size_t)p->merge_items);
+    }
+    p->table_offset = p->node_bytes + p->work_bytes + p->leaf_list_bytes;
+    p->prec_offset = p->table_offset + p->table_bytes;
+    p->crec_offset = p->prec_offset + p->prec_bytes;
+    p->arena_offset = p->crec_offset + p->crec_bytes;
     p->arena_bytes = arena;
     p->total_bytes = p->arena_offset + arena;
-    p->launches = p->max_height + 1 + (mode == SARBP_SPLIT ? 1 : 0);
+    p->launches = p->max_height + 1 + (mode == SARBP_SPLIT ? 3 : 0);
     *plan_out = p;
     return SARBP_OK;
 }
@@ -472,6 +492,9 @@ int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_byt
             e = cudaMemcpyAsync(base + plan->node_bytes, plan->blocks.data(), sizeof(int2) * plan->blocks.size(),
                                 cudaMemcpyHostToDevice, s);
     }
+    if (e == cudaSuccess && !plan->leaves.empty())
+        e = cudaMemcpyAsync(base + plan->node_bytes + plan->work_bytes, plan->leaves.data(),
+                            sizeof(int) * plan->leaves.size(), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "FFBP bind: %s", cudaGetErrorString(e));
     plan->bound = workspace;
@@ -498,24 +521,31 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
     int st = SARBP_OK;
     if (plan->mode == SARBP_SPLIT) {
         const TileItem* items = reinterpret_cast<const TileItem*>(base + plan->node_bytes);
-        // leaf_wb was sized for unit sample spacing; rescale to this data_dr.
-        double rad = 0.0;
-        for (int i = 0; i < plan->n_nodes; ++i)
-            if (plan->nodes[i].left < 0) {
-                double r = 0.0;
-                split_polar_tile_lc(plan->nodes[i], &r);
-                rad = std::max(rad, r);
-            }
-        const int wb = split_window_bins(rad, data_dr);
-        const int ch = split_chunk_for(wb, plan->leaf_chunk);
+        const int* leaves = reinterpret_cast<const int*>(base + plan->node_bytes + plan->work_bytes);
         float4* tables = reinterpret_cast<float4*>(base + plan->table_offset);
-        st = launch_split_ffbp_tables(k, nodes, plan->n_nodes, plan->max_dim, tables, s);
+        void* precs = base + plan->prec_offset;
+        void* crecs = base + plan->crec_offset;
+        // A 32-row leaf tile spans 32 dr of range; pulses add their offset from the leaf centre.
+        double span = 0.0;
+        for (int i : plan->leaves) span = std::max(span, 32.0 * fabs(plan->nodes[i].dr));
+        const int wb = (int)ceil(span / fabs(data_dr)) + 48;
+        const int ch = split_chunk_for(wb, plan->leaf_chunk);
+        st = launch_split_ffbp_tables(in, nodes, plan->n_nodes, plan->max_dim, tables, s);
+        if (st == SARBP_OK)
+            st = launch_split_ffbp_leaf_pulses(in, nodes, leaves, (int)plan->leaves.size(), precs, s);
+        if (st == SARBP_OK)
+            st = launch_split_ffbp_child_records(k, nodes, items + plan->stage_begin[0] + plan->stage_count[0],
+                                                 (int)plan->merge_items, arena, crecs, s);
         if (st == SARBP_OK)
             st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb,
-                                          tables, arena, root_out, 0, s);
-        for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h)
-            st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables, arena,
-                                          root_out, 0, s);
+                                          tables, precs, arena, root_out, 0, s);
+        const size_t crec_size = split_ffbp_child_record_bytes();
+        for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h) {
+            const size_t first = (size_t)(plan->stage_begin[h] - plan->stage_begin[1]);
+            st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables,
+                                          reinterpret_cast<char*>(crecs) + 2 * first * crec_size, arena, root_out, 0,
+                                          s);
+        }
     } else {
         const int2* blocks = reinterpret_cast<const int2*>(base + plan->node_bytes);
         st = launch_plain_ffbp_leaves(plan->mode, in, nodes, blocks + plan->stage_begin[0], plan->stage_count[0],

@@ -158,13 +158,22 @@ int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pu
                          int window_bins, float2* out, long long split_stride, cudaStream_t s);
 int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
                         int window_bins, float2* out, long long split_stride, cudaStream_t s);
-// Per-node row/column geometry tables for the FFBP split kernels (one launch per execute).
-int launch_split_ffbp_tables(double k, const PolarDesc* nodes, int n_nodes, int max_dim, float4* tables,
-                             cudaStream_t s);
+// FFBP split path: per-node row/column geometry tables (3 float4 per row, 1 per
+// column), per-pulse leaf records and per-(merge tile, child) records, computed
+// by three prologue launches per execute.
+int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int n_nodes, int max_dim,
+                             float4* tables, cudaStream_t s);
+int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes, const int* leaves, int n_leaves,
+                                  void* recs, cudaStream_t s);
+int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const TileItem* items, int n_items,
+                                    float2* arena, void* recs, cudaStream_t s);
+size_t split_ffbp_pulse_record_bytes();
+size_t split_ffbp_child_record_bytes();
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             int chunk, int window_bins, const float4* tables, float2* arena, float2* root_out,
-                             int root, cudaStream_t s);
+                             int chunk, int window_bins, const float4* tables, const void* precs, float2* arena,
+                             float2* root_out, int root, cudaStream_t s);
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             const float4* tables, float2* arena, float2* root_out, int root, cudaStream_t s);
+                             const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
+                             cudaStream_t s);
 
 }  // namespace sarbp

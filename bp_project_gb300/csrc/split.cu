@@ -257,9 +257,11 @@ __device__ void setup_polar(const SplitParams& P, const Job& J, TileShared& S, P
 }
 
 // Polar tile set-up from per-node FP64 tables stored as float pairs (FFBP):
-// FP32 two-float arithmetic only, no block reductions.  Row i holds
-// (g_i hi, g_i lo, psi_i) with g = sqrt(r^2 - oz^2) and psi = frac(-K r);
-// column j holds (c_j hi, c_j lo, u_j hi, u_j lo) with c = sqrt(1 - u^2).
+// FP32 two-float arithmetic only, no block reductions.  Row i holds three
+// float4: (g hi, g lo, psi, 0), (g/r hi, g/r lo, -oz/r hi, -oz/r lo) and
+// (2r, frac(Q) - 1/2, floor(Q) bits, 0) with g = sqrt(r^2 - oz^2),
+// psi = frac(-K r) and Q = (r - range_start) / data_dr; column j holds
+// (c hi, c lo, u hi, u lo) with c = sqrt(1 - u^2).
 struct TabF {
     float rxh[kMaxRows], rxl[kMaxRows], ryh[kMaxRows], ryl[kMaxRows], dg[kMaxRows], psi[kMaxRows];
     float cxh[kMaxCols], cxl[kMaxCols], cyh[kMaxCols], cyl[kMaxCols], dcs[kMaxCols], duu[kMaxCols];
@@ -286,12 +288,12 @@ __device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const floa
     const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
     const int i0 = min(g.win_r0 + J.tile_r + (rows_t >> 1), g.nr - 1);
     const int j0 = min(g.win_u0 + J.tile_u + (cols_t >> 1), g.nu - 1);
-    const float4 r0v = __ldg(tables + g.rows_off + i0);
+    const float4 r0v = __ldg(tables + g.rows_off + 3 * (long long)i0);
     const float4 c0v = __ldg(tables + g.cols_off + j0);
     const float side = (float)g.side;
     if (tid < rows_t) {
         const int i = min(g.win_r0 + J.tile_r + tid, g.nr - 1);
-        const float4 rv = __ldg(tables + g.rows_off + i);
+        const float4 rv = __ldg(tables + g.rows_off + 3 * (long long)i);
         const float dh = rv.x - r0v.x, dl = rv.y - r0v.y;  // g values of one node: dh is exact
         float p, e;
         two_prod(dh, dl, c0v.x, c0v.y, p, e);
@@ -720,32 +722,9 @@ __global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P
     }
 }
 
-// ---- FFBP: leaves ---------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
-                                                                 const TileItem* __restrict__ items,
-                                                                 const float4* __restrict__ tables,
-                                                                 float2* __restrict__ arena, float2* root_out,
-                                                                 int root) {
-    extern __shared__ __align__(16) char smem[];
-    __shared__ TileShared S;
-    const TileItem it = items[blockIdx.x];
-    Job J;
-    J.g = nodes[it.node];
-    J.lc = J.g.tile_lc;
-    J.tile_r = it.tile_r;
-    J.tile_u = it.tile_u;
-    J.p0 = J.g.a;
-    J.p1 = J.g.b;
-    Pix px[kPX];
-    TabF& T = *reinterpret_cast<TabF*>(smem + (size_t)kMaxChunk * sizeof(Rec));
-    setup_polar_tab(J, S, T, tables, px);
-    pulse_loop<false, true>(P, J, S, smem, px);
-    float2* dst = it.node == root ? root_out : arena + J.g.out_offset;
-    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
-}
-
-// Per-node geometry tables (FP64 once per row / column, stored as float pairs).
-__global__ void ffbp_tables_kernel(double K, const PolarDesc* __restrict__ nodes, float4* __restrict__ tables) {
+// ---- FFBP: per-node tables and per-pulse leaf records (prologue kernels) ------------------
+__global__ void ffbp_tables_kernel(double K, double range_start, double inv_dr, const PolarDesc* __restrict__ nodes,
+                                   float4* __restrict__ tables) {
     const PolarDesc& g = nodes[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < g.nr) {
@@ -753,13 +732,259 @@ __global__ void ffbp_tables_kernel(double K, const PolarDesc* __restrict__ nodes
         const double gg = sqrt(fmax(0.0, r * r - g.oz * g.oz));
         const float gh = (float)gg;
         const double ph = -K * r;
-        tables[g.rows_off + t] = make_float4(gh, (float)(gg - (double)gh), (float)(ph - rint(ph)), 0.0f);
+        const double gr = gg / r, ez = -g.oz / r;
+        const float grh = (float)gr, ezh = (float)ez;
+        const double Q = (r - range_start) * inv_dr;
+        const double I = fmin(fmax(floor(Q), -1.0e9), 1.0e9);
+        float4* row = tables + g.rows_off + 3 * (long long)t;
+        row[0] = make_float4(gh, (float)(gg - (double)gh), (float)(ph - rint(ph)), 0.0f);
+        row[1] = make_float4(grh, (float)(gr - (double)grh), ezh, (float)(ez - (double)ezh));
+        row[2] = make_float4((float)(2.0 * r), (float)(Q - I - 0.5), __int_as_float((int)I), 0.0f);
     }
     if (t < g.nu) {
         const double u = g.u0 + (double)t * g.du;
         const double c = sqrt(fmax(0.0, 1.0 - u * u));
         const float chh = (float)c, uh = (float)u;
         tables[g.cols_off + t] = make_float4(chh, (float)(c - (double)chh), uh, (float)(u - (double)uh));
+    }
+}
+
+// Leaf pulses relative to the leaf's phase centre O (origin formulation).
+// A = -K (pos - O) is split into a multiple of a per-leaf power-of-two
+// quantum with <= 10 significant bits plus an FP32 remainder.
+struct PulseRec {
+    float4 a;  // A_hi.x, A_hi.y, A_hi.z, frac(phase / 2pi)
+    float4 b;  // A_lo.x, A_lo.y, A_lo.z, |pos - O|^2
+    float4 c;  // (pos - O).x, .y, .z, weight
+};
+
+__global__ void ffbp_leaf_pulses_kernel(double K, const double* __restrict__ pos, const double* __restrict__ weight,
+                                        const double* __restrict__ phase, const PolarDesc* __restrict__ nodes,
+                                        const int* __restrict__ leaves, PulseRec* __restrict__ recs) {
+    __shared__ int amax;
+    const PolarDesc& g = nodes[leaves[blockIdx.x]];
+    if (threadIdx.x == 0) amax = 0;
+    __syncthreads();
+    float m = 0.0f;
+    for (int n = g.a + threadIdx.x; n < g.b; n += blockDim.x) {
+        const double ax = pos[3 * n] - g.ox, ay = pos[3 * n + 1] - g.oy, az = pos[3 * n + 2] - g.oz;
+        m = fmaxf(m, (float)(fabs(K) * fmax(fabs(ax), fmax(fabs(ay), fabs(az)))));
+    }
+    atomicMax(&amax, __float_as_int(m));  // non-negative floats order like their bit patterns
+    __syncthreads();
+    int e = 0;
+    frexp((double)__int_as_float(amax) * 1.0001 + 1e-30, &e);
+    const double scale = ldexp(1.0, e - 10), inv_scale = ldexp(1.0, 10 - e);
+    for (int n = g.a + threadIdx.x; n < g.b; n += blockDim.x) {
+        const double ax = pos[3 * n] - g.ox, ay = pos[3 * n + 1] - g.oy, az = pos[3 * n + 2] - g.oz;
+        PulseRec r;
+        quantize(-K * ax, scale, inv_scale, r.a.x, r.b.x);
+        quantize(-K * ay, scale, inv_scale, r.a.y, r.b.y);
+        quantize(-K * az, scale, inv_scale, r.a.z, r.b.z);
+        const double t = phase[n] * kInvTwoPi;
+        r.a.w = (float)(t - rint(t));
+        r.b.w = (float)(ax * ax + ay * ay + az * az);
+        r.c = make_float4((float)ax, (float)ay, (float)az, (float)weight[n]);
+        recs[n] = r;
+    }
+}
+
+// ---- FFBP: leaves (origin formulation) ---------------------------------------------------
+//
+// With O the leaf's phase centre and a = pos_n - O (|a| ~ the leaf aperture),
+// a pixel at slant range r from O in unit direction e satisfies exactly
+//   d = |r e - a| = r - L + eps,  L = e . a,  eps = (|a|^2 - L^2) / (2 (r - L) + eps),
+// so the demodulated phase k (d - r) + phase_n is -K e . a + K eps + phase_n / 2pi
+// (turns): no large term, no per-tile FP64.  e comes from the row / column
+// tables as a quantized pair (2^-11), so A_hi . e_hi is exact.
+struct LeafRec {
+    float4 a;  // A_hi.x, A_hi.y, A_hi.z, Phi
+    float4 b;  // A_lo.x, A_lo.y, A_lo.z, |a|^2
+    float4 c;  // a.x, a.y, a.z, window bias bits
+    float4 d;  // window offset bits, window count - 1 bits
+};
+
+struct LPix {
+    float ex, ey, ez, exh, eyh, ezh, exl, eyl, ezl;
+    float r2, fm;
+    int rowoff;
+    float ar, ai;
+};
+
+constexpr float kUnitQ = 1.0f / 2048.0f;  // quantum of unit-vector components (11 bits)
+
+__device__ __forceinline__ void unit_pair(float p, float e, float& h, float& l, float& full) {
+    h = rintf(p * 2048.0f) * kUnitQ;
+    l = (p - h) + e;
+    full = p + e;
+}
+
+__global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+                                                                 const TileItem* __restrict__ items,
+                                                                 const float4* __restrict__ tables,
+                                                                 const PulseRec* __restrict__ precs,
+                                                                 float2* __restrict__ arena, float2* root_out,
+                                                                 int root) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ int s_base[kMaxChunk];
+    __shared__ float s_wt[kMaxChunk];
+    __shared__ int s_nfit;
+    const TileItem it = items[blockIdx.x];
+    const PolarDesc g = nodes[it.node];
+    const int lc = g.tile_lc, cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float side = (float)g.side;
+    const int ifirst = min(g.win_r0 + it.tile_r, g.nr - 1);
+    const int ilast = min(g.win_r0 + it.tile_r + rows_t - 1, g.nr - 1);
+    const float4 rfirst = __ldg(tables + g.rows_off + 3 * (long long)ifirst + 2);
+    const int I_first = __float_as_int(rfirst.z);
+    const int I_span = __float_as_int(__ldg(tables + g.rows_off + 3 * (long long)ilast + 2).z) - I_first;
+    const float r_min = 0.5f * rfirst.x;
+    LPix px[kPX];
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = tid + kThreads * k;
+        const int i = min(g.win_r0 + it.tile_r + (p >> lc), g.nr - 1);
+        const int j = min(g.win_u0 + it.tile_u + (p & (cols_t - 1)), g.nu - 1);
+        const float4 r1 = __ldg(tables + g.rows_off + 3 * (long long)i + 1);
+        const float4 r2 = __ldg(tables + g.rows_off + 3 * (long long)i + 2);
+        const float4 cv = __ldg(tables + g.cols_off + j);
+        LPix& q = px[k];
+        float pp, ee;
+        two_prod(r1.x, r1.y, cv.x, cv.y, pp, ee);
+        unit_pair(side * pp, side * ee, q.exh, q.exl, q.ex);
+        two_prod(r1.x, r1.y, cv.z, cv.w, pp, ee);
+        unit_pair(pp, ee, q.eyh, q.eyl, q.ey);
+        unit_pair(r1.z, r1.w, q.ezh, q.ezl, q.ez);
+        q.r2 = r2.x;
+        q.fm = r2.y;
+        q.rowoff = __float_as_int(r2.z) - I_first;
+        q.ar = q.ai = 0.0f;
+    }
+    LeafRec* rec = reinterpret_cast<LeafRec*>(smem);
+    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxChunk * sizeof(LeafRec));
+    const PulseInputs& in = P.in;
+    const float inv_dr = P.inv_drf, Kf = P.Kf;
+    for (int c0 = g.a; c0 < g.b;) {
+        const int want = min(P.chunk, g.b - c0);
+        __syncthreads();
+        if (warp == 0) {
+            int count = 0;
+            if (lane < want) {
+                const PulseRec pr = precs[c0 + lane];
+                const float amag = sqrtf(pr.b.w);
+                const float eps_max = pr.b.w / (2.0f * fmaxf(r_min - amag, 1.0f));
+                const float hw = (amag + eps_max) * fabsf(inv_dr) + 1e-3f;
+                const int bo = (int)floorf(-0.5f - hw), top = (int)ceilf(0.5f + hw);
+                const long long cnt = (long long)I_span + top - bo + 1;
+                count = cnt <= P.cap ? (int)cnt : P.cap + 1;
+                s_base[lane] = I_first + bo;
+                s_wt[lane] = pr.c.w;
+                LeafRec r;
+                r.a = pr.a;
+                r.b = pr.b;
+                r.c = make_float4(pr.c.x, pr.c.y, pr.c.z, __int_as_float(kMagicBits + bo));
+                r.d = make_float4(0.0f, __int_as_float(count - 1), 0.0f, 0.0f);
+                rec[lane] = r;
+            }
+            int inc = count;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            const unsigned fits = __ballot_sync(0xffffffffu, lane < want && inc <= P.cap);
+            if (lane < want) rec[lane].d.x = __int_as_float(inc - count);
+            if (lane == 0) s_nfit = __popc(fits);
+        }
+        __syncthreads();
+        const int nfit = s_nfit;
+        const int chn = nfit > 0 ? nfit : 1;
+        if (nfit > 0) {
+            for (int nl = warp; nl < nfit; nl += kThreads / 32) {
+                const int off = __float_as_int(rec[nl].d.x);
+                const int cnt = __float_as_int(rec[nl].d.y) + 1;
+                const long long b0 = s_base[nl];
+                const float a = s_wt[nl];
+                const float2* row = in.data + (size_t)(c0 + nl) * in.samples;
+                for (int jj = lane; jj < cnt; jj += 32) {
+                    const long long gb = b0 + jj;
+                    float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
+                    if (gb >= 1 && gb <= (long long)in.samples - 3)
+                        cubic_coefficients(__ldg(row + gb - 1), __ldg(row + gb), __ldg(row + gb + 1), __ldg(row + gb + 2),
+                                           a, c01, c23);
+                    win[2 * (off + jj)] = c01;
+                    win[2 * (off + jj) + 1] = c23;
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll 1
+        for (int nl = 0; nl < chn; ++nl) {
+            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+            const int bias = __float_as_int(rc.w);
+            const unsigned last = (unsigned)__float_as_int(rd.y);
+            const float4* wrow = win + 2 * __float_as_int(rd.x);
+            const float2* drow = in.data + (size_t)(c0 + nl) * in.samples;
+#pragma unroll
+            for (int k = 0; k < kPX; ++k) {
+                LPix& q = px[k];
+                const float L = fmaf(rc.x, q.ex, fmaf(rc.y, q.ey, rc.z * q.ez));
+                const float q2 = fmaf(-L, L, rb.w);
+                const float B = rcp_approx(fmaf(-2.0f, L, q.r2));
+                const float e0 = q2 * B;
+                const float eps = fmaf(-e0 * e0, B, e0);  // second order: leaves can be tens of metres wide
+                const float qp = fmaf(eps - L, inv_dr, q.fm);
+                const float tq = qp + kMagic;
+                const float s = qp - (tq - kMagic);
+                float vr, vi;
+                if (nfit > 0) {
+                    const unsigned j = min((unsigned)(__float_as_int(tq) + q.rowoff - bias), last);
+                    const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                    vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+                    vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+                } else {  // the pulse's window does not fit: gather its taps directly
+                    const long long gb = (long long)(__float_as_int(tq) - kMagicBits) + q.rowoff + I_first;
+                    vr = vi = 0.0f;
+                    if (gb >= 1 && gb <= (long long)in.samples - 3) {
+                        float w[4];
+                        lagrange_centred(s, w);
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            const float2 v = __ldg(drow + gb + b - 1);
+                            vr = fmaf(w[b], v.x, vr);
+                            vi = fmaf(w[b], v.y, vi);
+                        }
+                        vr *= s_wt[nl];
+                        vi *= s_wt[nl];
+                    }
+                }
+                float tb = fmaf(ra.x, q.exh, fmaf(ra.y, q.eyh, ra.z * q.ezh));  // exact
+                float sm = fmaf(Kf, eps, ra.w);
+                sm = fmaf(ra.x, q.exl, sm);
+                sm = fmaf(ra.y, q.eyl, sm);
+                sm = fmaf(ra.z, q.ezl, sm);
+                sm = fmaf(rb.x, q.ex, sm);
+                sm = fmaf(rb.y, q.ey, sm);
+                sm = fmaf(rb.z, q.ez, sm);
+                const float tot = (tb - round_magic(tb)) + sm;
+                const float ang = (tot - round_magic(tot)) * kTwoPiF;
+                float sn, cs;
+                __sincosf(ang, &sn, &cs);
+                q.ar = fmaf(vr, cs, q.ar);
+                q.ar = fmaf(-vi, sn, q.ar);
+                q.ai = fmaf(vr, sn, q.ai);
+                q.ai = fmaf(vi, cs, q.ai);
+            }
+        }
+        c0 += chn;
+    }
+    float2* dst = it.node == root ? root_out : arena + g.out_offset;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = tid + kThreads * k;
+        const int wr = it.tile_r + (p >> lc), wu = it.tile_u + (p & (cols_t - 1));
+        if (wr < g.win_nr && wu < g.win_nu) dst[(long long)wr * g.out_stride + wu] = make_float2(px[k].ar, px[k].ai);
     }
 }
 
@@ -774,21 +999,37 @@ struct ChildRec {
     const float2* img;
 };
 
-__device__ __forceinline__ void child_record(const SplitParams& P, const TileShared& S, const PolarDesc& c,
-                                             const float2* img, ChildRec& R) {
-    const double vx = S.cx - c.ox, vy = S.cy - c.oy, vz = S.cz - c.oz;
+// One thread per (merge tile, child): the tile centre is the FP64 position of
+// the tile's centre pixel, the same point setup_polar_tab measures offsets from.
+__global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_scale_w,
+                                          const PolarDesc* __restrict__ nodes, const TileItem* __restrict__ items,
+                                          int n_items, float2* __restrict__ arena, ChildRec* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * n_items) return;
+    const TileItem it = items[t >> 1];
+    const PolarDesc& g = nodes[it.node];
+    const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
+    const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
+    const int i0 = min(g.win_r0 + it.tile_r + (rows_t >> 1), g.nr - 1);
+    const int j0 = min(g.win_u0 + it.tile_u + (cols_t >> 1), g.nu - 1);
+    const double rc = g.r0 + (double)i0 * g.dr;
+    const double g0 = sqrt(fmax(0.0, rc * rc - g.oz * g.oz));
+    const double uc = g.u0 + (double)j0 * g.du;
+    const double c0 = sqrt(fmax(0.0, 1.0 - uc * uc));
+    const double vx = g.ox + (double)g.side * g0 * c0 - c.ox, vy = g.oy + g0 * uc - c.oy, vz = -c.oz;
     const double g2 = vx * vx + vy * vy;
     const double G = sqrt(g2);
     const double RR = sqrt(g2 + vz * vz);
     const double ux = vx / RR, uy = vy / RR;
-    const double t1 = P.K * RR;
+    const double t1 = K * RR;
     const double qr = (RR - c.r0) / c.dr;
     const double ir = floor(qr);
     const double hx = vx / G, hy = vy / G;
     const double qu = (hy - c.u0) / c.du;
     const double iu = floor(qu);
-    quantize(P.K * ux, P.scale_w, P.inv_scale_w, R.a.x, R.a.z);
-    quantize(P.K * uy, P.scale_w, P.inv_scale_w, R.a.y, R.a.w);
+    ChildRec R;
+    quantize(K * ux, scale_w, inv_scale_w, R.a.x, R.a.z);
+    quantize(K * uy, scale_w, inv_scale_w, R.a.y, R.a.w);
     R.b = make_float4((float)ux, (float)uy, (float)(2.0 * RR), (float)(qr - ir - 0.5));
     R.c = make_float4((float)(t1 - rint(t1)), (float)hx, (float)hy, (float)(2.0 * G));
     R.d = make_float4((float)G, (float)(qu - iu - 0.5), 0.0f, 0.0f);
@@ -799,7 +1040,8 @@ __device__ __forceinline__ void child_record(const SplitParams& P, const TileSha
     R.iu0 = ok ? (int)iu : -(1 << 30);
     R.snr = c.nr;
     R.snu = c.nu;
-    R.img = img;
+    R.img = arena + c.out_offset;
+    out[t] = R;
 }
 
 __device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildRec& R, const Pix& q) {
@@ -845,22 +1087,22 @@ __device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildR
         }
     }
     const float tb = fmaf(R.a.x, q.dxh, R.a.y * q.dyh);
-    const float fb = tb - round_magic(tb);
     float sm = fmaf(P.Kf, eps, R.c.x);
     sm = fmaf(R.a.x, q.dxl, sm);
     sm = fmaf(R.a.y, q.dyl, sm);
     sm = fmaf(R.a.z, q.dx, sm);
     sm = fmaf(R.a.w, q.dy, sm);
-    const float tot = (fb + q.psi) + sm;
+    const float tot = (tb - round_magic(tb)) + (sm + q.psi);
     const float ang = (tot - round_magic(tot)) * kTwoPiF;
     float sn, cs;
     __sincosf(ang, &sn, &cs);
     return make_float2(vr * cs - vi * sn, vr * sn + vi * cs);
 }
 
-__global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kThreads, 3) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
                                                                   const float4* __restrict__ tables,
+                                                                  const ChildRec* __restrict__ crecs,
                                                                   float2* __restrict__ arena, float2* root_out,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
@@ -872,15 +1114,10 @@ __global__ void __launch_bounds__(kThreads, 2) split_merge_kernel(SplitParams P,
     J.lc = J.g.tile_lc;
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
+    if (threadIdx.x < 2) C[threadIdx.x] = crecs[2 * (long long)blockIdx.x + threadIdx.x];
     Pix px[kPX];
     TabF& T = *reinterpret_cast<TabF*>(smem);
     setup_polar_tab(J, S, T, tables, px);
-    if (threadIdx.x < 2) {
-        const int child = threadIdx.x == 0 ? J.g.left : J.g.right;
-        const PolarDesc c = nodes[child];
-        child_record(P, S, c, arena + c.out_offset, C[threadIdx.x]);
-    }
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < kPX; ++k) {
         const float2 a = child_value(P, C[0], px[k]);
@@ -1028,32 +1265,56 @@ int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int 
     return check_launch("split_points");
 }
 
-int launch_split_ffbp_tables(double k, const PolarDesc* nodes, int n_nodes, int max_dim, float4* tables,
-                             cudaStream_t s) {
+int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int n_nodes, int max_dim,
+                             float4* tables, cudaStream_t s) {
     if (n_nodes <= 0) return SARBP_OK;
     dim3 grid((max_dim + kThreads - 1) / kThreads, n_nodes);
-    ffbp_tables_kernel<<<grid, kThreads, 0, s>>>(k * kInvTwoPi, nodes, tables);
+    ffbp_tables_kernel<<<grid, kThreads, 0, s>>>(in.k * kInvTwoPi, in.range_start, 1.0 / in.data_dr, nodes, tables);
     note_launches(1);
     return check_launch("split_ffbp_tables");
 }
 
+int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes, const int* leaves, int n_leaves,
+                                  void* recs, cudaStream_t s) {
+    if (n_leaves <= 0) return SARBP_OK;
+    ffbp_leaf_pulses_kernel<<<n_leaves, 128, 0, s>>>(in.k * kInvTwoPi, in.pos, in.weight, in.phase, nodes, leaves,
+                                                     reinterpret_cast<PulseRec*>(recs));
+    note_launches(1);
+    return check_launch("split_ffbp_leaf_pulses");
+}
+
+int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const TileItem* items, int n_items,
+                                    float2* arena, void* recs, cudaStream_t s) {
+    if (n_items <= 0) return SARBP_OK;
+    PulseInputs none{};
+    none.k = k;
+    none.data_dr = 1.0;
+    const SplitParams P = make_params(none, 1, 4, 1);
+    ffbp_child_records_kernel<<<grid_blocks(2LL * n_items, kThreads), kThreads, 0, s>>>(
+        P.K, P.scale_w, P.inv_scale_w, nodes, items, n_items, arena, reinterpret_cast<ChildRec*>(recs));
+    note_launches(1);
+    return check_launch("split_ffbp_child_records");
+}
+
+size_t split_ffbp_pulse_record_bytes() { return sizeof(PulseRec); }
+size_t split_ffbp_child_record_bytes() { return sizeof(ChildRec); }
+
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             int chunk, int window_bins, const float4* tables, float2* arena, float2* root_out,
-                             int root, cudaStream_t s) {
+                             int chunk, int window_bins, const float4* tables, const void* precs, float2* arena,
+                             float2* root_out, int root, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
-    P.envelope = kLeafEnvelope;
-    size_t smem = dynamic_smem(P.cap, false);
-    const size_t need = (size_t)kMaxChunk * sizeof(Rec) + sizeof(TabF);
-    if (smem < need) smem = need;
+    const size_t smem = (size_t)kMaxChunk * sizeof(LeafRec) + (size_t)P.cap * 32;
     if (int st = prepare(split_leaf_kernel, smem)) return st;
-    split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, arena, root_out, root);
+    split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const PulseRec*>(precs),
+                                                     arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_leaves");
 }
 
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
-                             const float4* tables, float2* arena, float2* root_out, int root, cudaStream_t s) {
+                             const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
+                             cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
@@ -1061,7 +1322,8 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
     SplitParams P = make_params(none, 1, 4, 1);
     const size_t smem = sizeof(TabF);
     if (int st = prepare(split_merge_kernel, smem)) return st;
-    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, arena, root_out, root);
+    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs),
+                                                      arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_merges");
 }

@@ -95,11 +95,11 @@ def test_ffbp_plan_object_on_host(golden, lib, mode):
     crop = (plan.crop_r[0], plan.crop_u[0], plan.nr, plan.nu)
     assert h.sarbp_ffbp_plan_create(arr, len(arr), *crop, lib.mode_id(mode), ctypes.byref(handle)) == 0
     # one launch for all leaves + one per tree height (8 merge levels for 256 leaves),
-    # plus the split path's per-node geometry table launch
-    assert h.sarbp_ffbp_launch_count(handle) == (10 if mode == "split" else 9)
+    # plus the split path's three prologue launches (geometry tables, leaf pulses, child records)
+    assert h.sarbp_ffbp_launch_count(handle) == (12 if mode == "split" else 9)
     ws = h.sarbp_ffbp_workspace_bytes(handle)
     images = sum(n.nr * n.nu * 8 for n in plan.nodes()[1:])
-    assert images <= ws <= images * 1.01 + (1 << 26)
+    assert images <= ws <= images * 1.06 + (1 << 26)  # + tables, tile records, node list
     # binding without a workspace is refused on the host
     assert h.sarbp_ffbp_bind(handle, None, 0, None) == lib.SARBP_ERR_WORKSPACE
     h.sarbp_ffbp_plan_destroy(handle)
