@@ -36,8 +36,12 @@ UNIT = "Gpixel·pulses/s"
 WORKLOAD = "c1 direct BP: 4096 pulses x 8192 bins -> 2048x2048 ground lattice @0.5 m, 9.6 GHz, split precision"
 FP32_FLOPS_PER_PX_PULSE = 54.0      # algorithmic FP32 work per pixel-pulse (FMA = 2)
 MUFU_PER_PX_PULSE = 3.0
-CPU_SAMPLE_PIXELS = 65536           # bounded CPU-baseline sample (all 4096 pulses)
-REF_SAMPLE_PIXELS = 32768           # pixels per step of the reference arm
+CPU_SAMPLE_PIXELS = 1 << 20         # bounded CPU-baseline sample (all 4096 pulses): ~10 s on 16 cores
+REF_SAMPLE_PIXELS = 131072          # pixels per step of the reference arm (~1 s on 16 cores)
+# DRAM bytes (read + write) of one split_lattice_kernel launch on this workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum): only the ~920 range bins per pulse that the scene spans
+# are read, so traffic is far below the algorithmic 302 MB.
+NCU_TRAFFIC_BYTES = 31.946752e6 + 2.132224e6
 
 
 def parse():
@@ -348,7 +352,7 @@ def main():
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                 "path": "pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), image -> host"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
                      "kernel": "split_lattice_kernel", "note": f"peak of {peak_kind}; algorithmic bytes "
                      f"{alg_bytes / 1e6:.1f} MB per launch; the kernel is FP32/MUFU-issue bound (roofline_fp32)"},
         "roofline_fp32": {"bound": "fp32_issue", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
