@@ -286,6 +286,35 @@ int sarbp_backproject_lattice(const float* data, int pulses, int samples, const 
     return st;
 }
 
+size_t sarbp_backproject_lattice_adjoint_workspace(const sarbp_lattice* lattice, int pulses) {
+    if (!lattice || lattice->rows <= 0 || lattice->cols <= 0 || pulses <= 0) return 0;
+    return split_adjoint_workspace(*lattice, pulses);
+}
+
+int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples, const double* pos,
+                                      const double* weight, const double* phase, const sarbp_lattice* lattice,
+                                      double range_start, double data_dr, double k, const float* grad_image,
+                                      double* grad_pos, double* grad_phase, double* grad_weight, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (!lattice || !grad_image) return fail(SARBP_ERR_TYPE, "lattice and grad_image must not be NULL");
+    if (!grad_pos && !grad_phase && !grad_weight) return fail(SARBP_ERR_VALUE, "no gradient requested");
+    if (lattice->rows <= 0 || lattice->cols <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    for (int c = 0; c < 3; ++c)
+        if (!is_finite_value(lattice->origin[c]) || !is_finite_value(lattice->step_row[c]) ||
+            !is_finite_value(lattice->step_col[c]))
+            return fail(SARBP_ERR_VALUE, "lattice geometry must be finite");
+    const size_t need = sarbp_backproject_lattice_adjoint_workspace(lattice, pulses);
+    if (!workspace || workspace_bytes < need)
+        return fail(SARBP_ERR_WORKSPACE, "backproject_lattice_adjoint needs %zu workspace bytes", need);
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    const int wb = split_window_bins(lattice_radius(*lattice, 5), data_dr);
+    const int ch = split_chunk_for(wb, 64);
+    return launch_split_lattice_adjoint(in, *lattice, ch, wb, reinterpret_cast<const float2*>(grad_image),
+                                        reinterpret_cast<float*>(workspace), grad_pos, grad_phase, grad_weight,
+                                        (cudaStream_t)stream);
+}
+
 // ---- FFBP building blocks ---------------------------------------------------------------
 int sarbp_regrid(const float* image, const sarbp_polar_grid* src, const sarbp_polar_grid* dst, double k, int mode,
                  float* out, void* stream) {

@@ -158,6 +158,13 @@ int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pu
                          int window_bins, float2* out, long long split_stride, cudaStream_t s);
 int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int pulse_split, int chunk,
                         int window_bins, float2* out, long long split_stride, cudaStream_t s);
+// Adjoint of split-precision lattice BP: per-pulse gradients of a real image loss
+// (grad = dl/dRe I + i dl/dIm I) with respect to position, phase and weight.
+size_t split_adjoint_workspace(const sarbp_lattice& lat, int pulses);
+int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat, int chunk, int window_bins,
+                                 const float2* grad, float* partials, double* grad_pos, double* grad_phase,
+                                 double* grad_weight, cudaStream_t s);
+
 // FFBP split path: per-node row/column geometry tables (3 float4 per row, 1 per
 // column), per-pulse leaf records and per-(merge tile, child) records, computed
 // by three prologue launches per execute.

@@ -584,8 +584,13 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
     return count;
 }
 
-template <bool HAS_Z, bool DEMOD>
-__device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, Pix px[kPX]) {
+// Chunk driver shared by the forward and adjoint kernels: per chunk, warp 0
+// computes the (tile, pulse) records and packs the pulses' range windows, all
+// warps stage the windows (Horner coefficients, times the pulse weight when
+// `weighted`), then `body.fast(rec, win, nfit, c0)` consumes them; a pulse
+// whose window cannot be staged goes through `body.slow(c0)`.
+template <class Body>
+__device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, bool weighted, Body& body) {
     const PulseInputs& in = P.in;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Rec* rec = reinterpret_cast<Rec*>(smem);
@@ -613,7 +618,7 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
                 const int off = __float_as_int(rec[nl].c.z);
                 const int cnt = __float_as_int(rec[nl].c.w) + 1;
                 const long long b0 = S.base[nl];
-                const float a = S.wt[nl];
+                const float a = weighted ? S.wt[nl] : 1.0f;
                 const float2* row = in.data + (size_t)(c0 + nl) * in.samples;
                 for (int j = lane; j < cnt; j += 32) {
                     const long long g = b0 + j;
@@ -626,23 +631,201 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
                 }
             }
             __syncthreads();
-            fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px);
+            body.fast(rec, win, nfit, c0);
             c0 += nfit;
         } else {
-#pragma unroll
-            for (int k = 0; k < kPX; ++k) {
-                Pix& q = px[k];
-                const float2 v = slow_pixel(in.data, in.samples, in.pos, in.weight, in.phase, in.range_start, P.inv_dr,
-                                            P.K, S.cx + ((double)q.dxh + (double)q.dxl),
-                                            S.cy + ((double)q.dyh + (double)q.dyl),
-                                            S.cz + ((double)q.dzh + (double)q.dzl), DEMOD ? q.psi : 0.0f, c0, 1);
-                q.ar += v.x;
-                q.ai += v.y;
-            }
+            body.slow(c0);
             c0 += 1;
         }
     }
 }
+
+template <bool HAS_Z, bool DEMOD>
+struct ForwardBody {
+    const SplitParams& P;
+    const TileShared& S;
+    Pix* px;
+    __device__ void fast(const Rec* rec, const float4* win, int nfit, int) { fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px); }
+    __device__ void slow(int c0) {
+        const PulseInputs& in = P.in;
+#pragma unroll
+        for (int k = 0; k < kPX; ++k) {
+            Pix& q = px[k];
+            const float2 v = slow_pixel(in.data, in.samples, in.pos, in.weight, in.phase, in.range_start, P.inv_dr, P.K,
+                                        S.cx + ((double)q.dxh + (double)q.dxl), S.cy + ((double)q.dyh + (double)q.dyl),
+                                        S.cz + ((double)q.dzh + (double)q.dzl), DEMOD ? q.psi : 0.0f, c0, 1);
+            q.ar += v.x;
+            q.ai += v.y;
+        }
+    }
+};
+
+template <bool HAS_Z, bool DEMOD>
+__device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, Pix px[kPX]) {
+    ForwardBody<HAS_Z, DEMOD> body{P, S, px};
+    chunk_loop(P, J, S, smem, true, body);
+}
+
+// ---- adjoint (gradients of a real image loss) -------------------------------------------
+//
+// With G_p = dl/dRe I_p + i dl/dIm I_p and c_pn = w_n v_pn exp(i phi_pn), the
+// per-pulse sums U_n = sum_p conj(G_p) v_pn exp(i phi_pn) and
+// A_n = sum_p Re(conj(G_p) (v'_pn / data_dr + i k v_pn) exp(i phi_pn)) e_pn
+// (e_pn the unit vector from pos_n to pixel p, v' = d sample1 / dq) give
+// dl/dpos_n = -w_n A_n, dl/dphase_n = -w_n Im U_n, dl/dweight_n = Re U_n.
+// Each CTA recomputes its tile's contributions and writes per-pulse partial
+// sums; adjoint_sum_kernel adds the tiles in fixed order.
+constexpr int kAdjVals = 5;  // Re U, Im U, A.x, A.y, A.z
+
+template <bool HAS_Z, bool DEMOD>
+struct AdjointBody {
+    const SplitParams& P;
+    const TileShared& S;
+    Pix* px;
+    const float* gre;
+    const float* gim;
+    float (*red)[kMaxChunk][kAdjVals];  // [warp][pulse][value]
+    float* part;                        // this tile's partial sums, [pulse][kAdjVals]
+    int pixels;                         // pixels of the tile that exist (the rest have G = 0)
+
+    __device__ void flush(int n0, int cnt) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt * kAdjVals; t += kThreads) {
+            const int nl = t / kAdjVals, v = t - nl * kAdjVals;
+            float acc = 0.0f;
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) acc += red[w][nl][v];
+            part[(size_t)(n0 + nl) * kAdjVals + v] = acc;
+        }
+    }
+
+    __device__ void fast(const Rec* rec, const float4* win, int nfit, int c0) {
+        const float inv_dr = P.inv_drf, Kf = P.Kf, kr = P.Kf * kTwoPiF;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+        for (int nl = 0; nl < nfit; ++nl) {
+            // rd.x (the unit vector's z) is needed for the z gradient even on a flat lattice.
+            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+            const int bias = __float_as_int(rc.y);
+            const unsigned last = (unsigned)__float_as_int(rc.w);
+            const float4* wrow = win + 2 * __float_as_int(rc.z);
+            const float R = 0.5f * rb.z;
+            float v5[kAdjVals] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < kPX; ++k) {
+                const Pix& q = px[k];
+                float L = fmaf(rb.x, q.dx, rb.y * q.dy);
+                if (HAS_Z) L = fmaf(rd.x, q.dz, L);
+                const float q2 = fmaf(-L, L, q.d2);
+                const float B = rcp_approx(fmaf(2.0f, L, rb.z));
+                const float e0 = q2 * B;
+                const float eps = fmaf(-e0 * e0, B, e0);
+                const float qp = fmaf(L + eps, inv_dr, rb.w);
+                const float tq = qp + kMagic;
+                const float s = qp - (tq - kMagic);
+                const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
+                const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+                const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+                const float dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
+                const float dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
+                float tb = ra.y * q.dyh;
+                if (HAS_Z) tb = fmaf(rd.y, q.dzh, tb);
+                tb = fmaf(ra.x, q.dxh, tb);
+                float sm = fmaf(Kf, eps, rc.x);
+                sm = fmaf(ra.x, q.dxl, sm);
+                sm = fmaf(ra.y, q.dyl, sm);
+                sm = fmaf(ra.z, q.dx, sm);
+                sm = fmaf(ra.w, q.dy, sm);
+                if (HAS_Z) {
+                    sm = fmaf(rd.y, q.dzl, sm);
+                    sm = fmaf(rd.z, q.dz, sm);
+                }
+                if (DEMOD) sm += q.psi;
+                const float tot = (tb - round_magic(tb)) + sm;
+                const float ang = (tot - round_magic(tot)) * kTwoPiF;
+                float sn, cs;
+                __sincosf(ang, &sn, &cs);
+                const float gr = gre[k], gi = gim[k];
+                const float er = vr * cs - vi * sn, ei = vr * sn + vi * cs;  // v exp(i phi)
+                v5[0] = fmaf(gr, er, fmaf(gi, ei, v5[0]));
+                v5[1] = fmaf(gr, ei, fmaf(-gi, er, v5[1]));
+                const float zr = fmaf(dvr, inv_dr, -kr * vi), zi = fmaf(dvi, inv_dr, kr * vr);
+                const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
+                const float t = fmaf(gr, fr, gi * fi) * rcp_approx(R + L + eps);
+                v5[2] = fmaf(t, fmaf(R, rb.x, q.dx), v5[2]);
+                v5[3] = fmaf(t, fmaf(R, rb.y, q.dy), v5[3]);
+                v5[4] = fmaf(t, fmaf(R, rd.x, q.dz), v5[4]);
+            }
+#pragma unroll
+            for (int v = 0; v < kAdjVals; ++v) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v5[v] += __shfl_xor_sync(0xffffffffu, v5[v], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int v = 0; v < kAdjVals; ++v) red[warp][nl][v] = v5[v];
+            }
+        }
+        flush(c0, nfit);
+    }
+
+    // A pulse whose window does not fit: per-sample FP64 geometry, FP32 interpolation.
+    __device__ void slow(int c0) {
+        const PulseInputs& in = P.in;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int n = c0;
+        const double pxn = in.pos[3 * n], pyn = in.pos[3 * n + 1], pzn = in.pos[3 * n + 2];
+        const double ph = in.phase[n] * kInvTwoPi;
+        const float2* row = in.data + (size_t)n * in.samples;
+        const float kr = P.Kf * kTwoPiF, inv_dr = P.inv_drf;
+        float v5[kAdjVals] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < kPX; ++k) {
+            const Pix& q = px[k];
+            const double x = S.cx + ((double)q.dxh + (double)q.dxl) - pxn;
+            const double y = S.cy + ((double)q.dyh + (double)q.dyl) - pyn;
+            const double z = S.cz + ((double)q.dzh + (double)q.dzl) - pzn;
+            const double d = sqrt(x * x + y * y + z * z);
+            const double t = P.K * d + ph;
+            const float tot = (float)(t - rint(t)) + (DEMOD ? q.psi : 0.0f);
+            const float ang = (tot - round_magic(tot)) * kTwoPiF;
+            const double qq = (d - in.range_start) * P.inv_dr;
+            const double fl = floor(qq);
+            if (!(fl >= 1.0 && fl <= (double)(in.samples - 3))) continue;
+            const int i = (int)fl;
+            const float2 x0 = __ldg(row + i - 1), x1 = __ldg(row + i), x2 = __ldg(row + i + 1), x3 = __ldg(row + i + 2);
+            float4 c01, c23;
+            cubic_coefficients(x0, x1, x2, x3, 1.0f, c01, c23);
+            const float s = (float)(qq - fl - 0.5);
+            const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+            const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+            const float dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
+            const float dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
+            float sn, cs;
+            __sincosf(ang, &sn, &cs);
+            const float gr = gre[k], gi = gim[k];
+            const float er = vr * cs - vi * sn, ei = vr * sn + vi * cs;
+            v5[0] = fmaf(gr, er, fmaf(gi, ei, v5[0]));
+            v5[1] = fmaf(gr, ei, fmaf(-gi, er, v5[1]));
+            const float zr = fmaf(dvr, inv_dr, -kr * vi), zi = fmaf(dvi, inv_dr, kr * vr);
+            const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
+            const float tt = fmaf(gr, fr, gi * fi) / (float)d;
+            v5[2] = fmaf(tt, (float)x, v5[2]);
+            v5[3] = fmaf(tt, (float)y, v5[3]);
+            v5[4] = fmaf(tt, (float)z, v5[4]);
+        }
+#pragma unroll
+        for (int v = 0; v < kAdjVals; ++v) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v5[v] += __shfl_xor_sync(0xffffffffu, v5[v], o);
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int v = 0; v < kAdjVals; ++v) red[warp][0][v] = v5[v];
+        }
+        flush(c0, 1);
+    }
+};
 
 // ---- output ----------------------------------------------------------------------
 __device__ __forceinline__ void store_window(const Job& J, int win_nr, int win_nu, const Pix px[kPX], float2* out,
@@ -720,6 +903,60 @@ __global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P
         const int idx = J.tile_r + threadIdx.x + kThreads * k;
         if (idx < npts) out[idx] = make_float2(px[k].ar, px[k].ai);
     }
+}
+
+// ---- adjoint kernels ----------------------------------------------------------------------
+template <bool HAS_Z>
+__global__ void __launch_bounds__(kThreads, 2) split_lattice_adjoint_kernel(SplitParams P, sarbp_lattice lat, int lc,
+                                                                            const float2* __restrict__ grad,
+                                                                            float* __restrict__ partials) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    __shared__ float red[kThreads / 32][kMaxChunk][kAdjVals];
+    Job J;
+    J.lat = lat;
+    J.lc = lc;
+    tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
+    J.p0 = 0;
+    J.p1 = P.in.pulses;
+    Pix px[kPX];
+    setup_lattice<HAS_Z>(J, S, px);
+    float gre[kPX], gim[kPX];
+    const int cols_t = 1 << lc;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = threadIdx.x + kThreads * k;
+        const int i = J.tile_r + (p >> lc), j = J.tile_u + (p & (cols_t - 1));
+        float2 g = make_float2(0.0f, 0.0f);
+        if (i < lat.rows && j < lat.cols) g = grad[(size_t)i * lat.cols + j];
+        gre[k] = g.x;
+        gim[k] = g.y;
+    }
+    AdjointBody<HAS_Z, false> body{P, S, px, gre, gim, red,
+                                   partials + (size_t)blockIdx.x * P.in.pulses * kAdjVals, kSplitTilePixels};
+    chunk_loop(P, J, S, smem, false, body);
+}
+
+// Per-pulse gradients from the tiles' partial sums, added in tile order (deterministic).
+__global__ void adjoint_sum_kernel(const float* __restrict__ partials, int ntiles, int pulses,
+                                   const double* __restrict__ weight, double* grad_pos, double* grad_phase,
+                                   double* grad_weight) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= pulses) return;
+    double acc[kAdjVals] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int t = 0; t < ntiles; ++t) {
+        const float* p = partials + ((size_t)t * pulses + n) * kAdjVals;
+#pragma unroll
+        for (int v = 0; v < kAdjVals; ++v) acc[v] += (double)p[v];
+    }
+    const double w = weight[n];
+    if (grad_pos) {
+        grad_pos[3 * n] = -w * acc[2];
+        grad_pos[3 * n + 1] = -w * acc[3];
+        grad_pos[3 * n + 2] = -w * acc[4];
+    }
+    if (grad_phase) grad_phase[n] = -w * acc[1];
+    if (grad_weight) grad_weight[n] = acc[0];
 }
 
 // ---- FFBP: per-node tables and per-pulse leaf records (prologue kernels) ------------------
@@ -1263,6 +1500,33 @@ int launch_split_points(const PulseInputs& in, const double* xyz, int npts, int 
     split_points_kernel<<<grid, kThreads, smem, s>>>(P, xyz, npts);
     note_launches(1);
     return check_launch("split_points");
+}
+
+size_t split_adjoint_workspace(const sarbp_lattice& lat, int pulses) {
+    return (size_t)tiles_of(lat.rows, lat.cols, 5) * (size_t)pulses * kAdjVals * sizeof(float);
+}
+
+int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat, int chunk, int window_bins,
+                                 const float2* grad, float* partials, double* grad_pos, double* grad_phase,
+                                 double* grad_weight, cudaStream_t s) {
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
+    const int lc = 5;
+    const size_t smem = dynamic_smem(P.cap, false);
+    const int ntiles = tiles_of(lat.rows, lat.cols, lc);
+    const bool has_z = lat.step_row[2] != 0.0 || lat.step_col[2] != 0.0;
+    if (has_z) {
+        if (int st = prepare(split_lattice_adjoint_kernel<true>, smem)) return st;
+        split_lattice_adjoint_kernel<true><<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
+    } else {
+        if (int st = prepare(split_lattice_adjoint_kernel<false>, smem)) return st;
+        split_lattice_adjoint_kernel<false><<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
+    }
+    note_launches(1);
+    if (int st = check_launch("split_lattice_adjoint")) return st;
+    adjoint_sum_kernel<<<grid_blocks(in.pulses, kThreads), kThreads, 0, s>>>(partials, ntiles, in.pulses, in.weight,
+                                                                            grad_pos, grad_phase, grad_weight);
+    note_launches(1);
+    return check_launch("adjoint_sum");
 }
 
 int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int n_nodes, int max_dim,

@@ -163,6 +163,25 @@ int sarbp_backproject_lattice(const float* data, int pulses, int samples, const 
                               double range_start, double data_dr, double k, int mode, int pulse_split,
                               float* out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- adjoint (differentiable BP) ------------------------------------------- */
+
+/* Gradients of a real loss l(I) of the split-precision lattice image with
+ * respect to the per-pulse inputs.  grad_image is complex64 [rows, cols] holding
+ * dl/dRe I + i dl/dIm I (torch's gradient of a real loss of a complex tensor).
+ * Outputs (any may be NULL, not all): grad_pos float64 [pulses, 3],
+ * grad_phase float64 [pulses], grad_weight float64 [pulses].  The kernel
+ * recomputes every pixel-pulse contribution (nothing is stored by the forward
+ * pass) and sums per-tile partials in fixed order.  No counterpart in the
+ * reference (its autofocus, fast_bp/autofocus.py:37-79, estimates phase
+ * gradients from target contributions instead); it drives gradient-based
+ * entropy autofocus. */
+size_t sarbp_backproject_lattice_adjoint_workspace(const sarbp_lattice* lattice, int pulses);
+int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples, const double* pos,
+                                      const double* weight, const double* phase, const sarbp_lattice* lattice,
+                                      double range_start, double data_dr, double k, const float* grad_image,
+                                      double* grad_pos, double* grad_phase, double* grad_weight, void* workspace,
+                                      size_t workspace_bytes, void* stream);
+
 /* ---- FFBP building blocks (eager schedule) -------------------------------- */
 
 /* Child polar image -> parent polar grid with 4x4 Lagrange and exp(j k (rr-r)).

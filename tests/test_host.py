@@ -67,6 +67,12 @@ def test_capi_rejects_bad_arguments_before_touching_the_gpu(lib):
                                       None) == lib.SARBP_ERR_VALUE
     assert h.sarbp_ffbp_execute(None, fake, 8, 64, fake, fake, fake, 90.0, 0.5, 1.0, fake, None) == lib.SARBP_ERR_TYPE
     assert h.sarbp_direct_polar_workspace(3, ctypes.byref(g), 8, 4) == 4 * 16 * 16 * 8
+    lat = lib.lattice((0, 0, 0), (0.5, 0, 0), (0, 0.5, 0), 64, 64)
+    adj = [fake, 8, 64, fake, fake, fake, ctypes.byref(lat), 90.0, 0.5, -50.0, fake]
+    # 2 x 2 tiles of 32 x 32 pixels, 8 pulses, 5 partial sums each
+    assert h.sarbp_backproject_lattice_adjoint_workspace(ctypes.byref(lat), 8) == 4 * 8 * 5 * 4
+    assert h.sarbp_backproject_lattice_adjoint(*adj, None, None, None, fake, 1 << 20, None) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_backproject_lattice_adjoint(*adj, fake, None, None, fake, 16, None) == lib.SARBP_ERR_WORKSPACE
 
 
 def _node_array(lib, plan):
