@@ -78,6 +78,8 @@ SIGNATURES = {
     "sarbp_backproject_lattice_adjoint_workspace": ([ctypes.POINTER(Lattice), _I], _Z),
     "sarbp_backproject_lattice_adjoint": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(Lattice), _D, _D, _D, _P, _P, _P, _P,
                                            _P, _Z, _P], _I),
+    "sarbp_sosfiltfilt_workspace": ([_I, _I, _I], _Z),
+    "sarbp_sosfiltfilt": ([_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _Z, _P], _I),
     "sarbp_regrid": ([_P, ctypes.POINTER(PolarGrid), ctypes.POINTER(PolarGrid), _D, _I, _P, _P], _I),
     "sarbp_merge_regrid": ([_P, ctypes.POINTER(PolarGrid), _P, ctypes.POINTER(PolarGrid), ctypes.POINTER(PolarGrid),
                             _D, _I, _P, _P], _I),

@@ -315,6 +315,28 @@ int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples
                                         (cudaStream_t)stream);
 }
 
+size_t sarbp_sosfiltfilt_workspace(int rows, int n, int padlen) {
+    if (rows <= 0 || n <= 0 || padlen < 0) return 0;
+    return sosfiltfilt_workspace(rows, n, padlen);
+}
+
+int sarbp_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections,
+                      const double* sos_host, int padlen, double* y, void* workspace, size_t workspace_bytes,
+                      void* stream) {
+    if (!x || !sos || !zi || !y) return fail(SARBP_ERR_TYPE, "x, sos, zi and y must be device pointers");
+    if (rows < 1 || n < 1) return fail(SARBP_ERR_VALUE, "x must have at least one row and one sample");
+    if (sections < 1 || sections > 8) return fail(SARBP_ERR_VALUE, "1 to 8 second-order sections are supported (got %d)", sections);
+    if (padlen < 0 || n <= padlen)
+        return fail(SARBP_ERR_VALUE, "the length of the input vector x must be greater than padlen, which is %d", padlen);
+    if (sos_host)
+        for (int s = 0; s < sections; ++s)
+            if (sos_host[6 * s + 3] != 1.0) return fail(SARBP_ERR_VALUE, "sos[:, 3] should be all ones");
+    const size_t need = sarbp_sosfiltfilt_workspace(rows, n, padlen);
+    if (!workspace || workspace_bytes < need) return fail(SARBP_ERR_WORKSPACE, "sosfiltfilt needs %zu workspace bytes", need);
+    return launch_sosfiltfilt(x, rows, n, sos, zi, sections, padlen, y, reinterpret_cast<double*>(workspace),
+                              (cudaStream_t)stream);
+}
+
 // ---- FFBP building blocks ---------------------------------------------------------------
 int sarbp_regrid(const float* image, const sarbp_polar_grid* src, const sarbp_polar_grid* dst, double k, int mode,
                  float* out, void* stream) {

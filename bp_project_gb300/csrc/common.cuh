@@ -165,6 +165,11 @@ int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat
                                  const float2* grad, float* partials, double* grad_pos, double* grad_phase,
                                  double* grad_weight, cudaStream_t s);
 
+// Zero-phase IIR smoothing along rows (autofocus phase-history filter).
+size_t sosfiltfilt_workspace(int rows, int n, int padlen);
+int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,
+                       double* y, double* ws, cudaStream_t s);
+
 // FFBP split path: per-node row/column geometry tables (3 float4 per row, 1 per
 // column), per-pulse leaf records and per-(merge tile, child) records, computed
 // by three prologue launches per execute.

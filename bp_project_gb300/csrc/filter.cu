@@ -1,0 +1,116 @@
+// Zero-phase IIR smoothing of per-target pulse histories for the phase-gradient
+// autofocus (fast_bp/autofocus.py:38-39: butter(4, cutoff) as second-order
+// sections, then sosfiltfilt along the pulse axis).
+//
+// Method: forward-backward filtering of an odd-extended signal with
+// steady-state initial conditions (Gustafsson's filtfilt, as published with
+// scipy.signal.sosfiltfilt): the row is extended by `padlen` samples at each
+// end with 2*x[end] - mirror, filtered forward through the cascade of
+// direct-form-II-transposed biquads starting from zi * first sample, then
+// filtered again over the reversed output starting from zi * its first
+// sample, and the extension is cut off.  The extension is formed in complex64
+// arithmetic like the reference's (its input is complex64); the filter runs
+// in FP64 with explicit roundings (no contraction).
+//
+// One thread per (row, real/imag) channel: the recursion is serial along the
+// pulses, the rows are independent.  The forward pass is kept in a
+// time-major workspace so that a warp's 32 channels touch consecutive words.
+#include "common.cuh"
+
+namespace sarbp {
+namespace {
+
+constexpr int kMaxSections = 8;
+
+__device__ __forceinline__ float extended(const float* x, int n, int padlen, int i, int comp) {
+    if (i < padlen) return __fsub_rn(2.0f * x[comp], x[2 * (padlen - i) + comp]);
+    const int j = i - padlen;
+    if (j < n) return x[2 * j + comp];
+    const int m = j - n;  // 0 .. padlen-1
+    return __fsub_rn(2.0f * x[2 * (n - 1) + comp], x[2 * (n - 2 - m) + comp]);
+}
+
+struct Biquads {
+    double b0[kMaxSections], b1[kMaxSections], b2[kMaxSections], a1[kMaxSections], a2[kMaxSections];
+    double z0[kMaxSections], z1[kMaxSections];
+    int sections;
+
+    __device__ double step(double v) {
+#pragma unroll
+        for (int s = 0; s < kMaxSections; ++s) {
+            if (s < sections) {
+                const double y = __dadd_rn(__dmul_rn(b0[s], v), z0[s]);
+                z0[s] = __dadd_rn(__dsub_rn(__dmul_rn(b1[s], v), __dmul_rn(a1[s], y)), z1[s]);
+                z1[s] = __dsub_rn(__dmul_rn(b2[s], v), __dmul_rn(a2[s], y));
+                v = y;
+            }
+        }
+        return v;
+    }
+};
+
+__global__ void sosfiltfilt_kernel(const float* __restrict__ x, int rows, int n, const double* __restrict__ sos,
+                                   const double* __restrict__ zi, int sections, int padlen, double* __restrict__ y,
+                                   double* __restrict__ ws) {
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    const int channels = 2 * rows;
+    if (ch >= channels) return;
+    const int row = ch >> 1, comp = ch & 1;
+    const float* xr = x + (size_t)row * n * 2;
+    const int m = n + 2 * padlen;
+    Biquads f;
+    f.sections = sections;
+    double zs0[kMaxSections], zs1[kMaxSections];
+#pragma unroll
+    for (int s = 0; s < kMaxSections; ++s) {
+        if (s < sections) {
+            f.b0[s] = sos[6 * s];
+            f.b1[s] = sos[6 * s + 1];
+            f.b2[s] = sos[6 * s + 2];
+            f.a1[s] = sos[6 * s + 4];  // a0 == 1 (checked by the caller)
+            f.a2[s] = sos[6 * s + 5];
+            zs0[s] = zi[2 * s];
+            zs1[s] = zi[2 * s + 1];
+        }
+    }
+    const double first = (double)extended(xr, n, padlen, 0, comp);
+#pragma unroll
+    for (int s = 0; s < kMaxSections; ++s) {
+        if (s < sections) {
+            f.z0[s] = __dmul_rn(zs0[s], first);
+            f.z1[s] = __dmul_rn(zs1[s], first);
+        }
+    }
+    for (int i = 0; i < m; ++i) ws[(size_t)i * channels + ch] = f.step((double)extended(xr, n, padlen, i, comp));
+    const double last = ws[(size_t)(m - 1) * channels + ch];
+#pragma unroll
+    for (int s = 0; s < kMaxSections; ++s) {
+        if (s < sections) {
+            f.z0[s] = __dmul_rn(zs0[s], last);
+            f.z1[s] = __dmul_rn(zs1[s], last);
+        }
+    }
+    double* yr = y + (size_t)row * n * 2;
+    for (int i = m - 1; i >= 0; --i) {
+        const double v = f.step(ws[(size_t)i * channels + ch]);
+        const int j = i - padlen;
+        if (j >= 0 && j < n) yr[2 * j + comp] = v;
+    }
+}
+
+}  // namespace
+
+size_t sosfiltfilt_workspace(int rows, int n, int padlen) {
+    return (size_t)(n + 2 * padlen) * (size_t)rows * 2 * sizeof(double);
+}
+
+int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,
+                       double* y, double* ws, cudaStream_t s) {
+    const int channels = 2 * rows;
+    const int block = 64;
+    sosfiltfilt_kernel<<<grid_blocks(channels, block), block, 0, s>>>(x, rows, n, sos, zi, sections, padlen, y, ws);
+    note_launches(1);
+    return check_launch("sosfiltfilt");
+}
+
+}  // namespace sarbp

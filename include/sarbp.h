@@ -182,6 +182,21 @@ int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples
                                       double* grad_pos, double* grad_phase, double* grad_weight, void* workspace,
                                       size_t workspace_bytes, void* stream);
 
+/* ---- autofocus helpers ---------------------------------------------------- */
+
+/* Zero-phase IIR filtering of each row of x (complex64 [rows, n]) with a
+ * cascade of `sections` second-order sections sos (float64 [sections, 6],
+ * b0 b1 b2 a0 a1 a2 with a0 = 1) and steady-state initial conditions zi
+ * (float64 [sections, 2]): odd extension by padlen samples, forward pass,
+ * backward pass, extension removed; y is complex128 [rows, n].  Replaces
+ * scipy.signal.sosfiltfilt(sos, xi, axis=1) in the phase-gradient autofocus
+ * (fast_bp/autofocus.py:38-39).  sos_host (optional) is a host copy of sos
+ * used only to check a0 == 1.  Requires n > padlen. */
+size_t sarbp_sosfiltfilt_workspace(int rows, int n, int padlen);
+int sarbp_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections,
+                      const double* sos_host, int padlen, double* y, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
 /* ---- FFBP building blocks (eager schedule) -------------------------------- */
 
 /* Child polar image -> parent polar grid with 4x4 Lagrange and exp(j k (rr-r)).

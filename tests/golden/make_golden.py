@@ -32,6 +32,15 @@ kernels.npz
 plans.npz
     ``build_ffbp_plan`` on the benchmark trajectories (1024 pulses / leaf 64
     and 4096 pulses / leaf 16) and on the validate.py track, flattened.
+autofocus.npz
+    ``autofocus.estimate_update`` (fast_bp/autofocus.py:37-79) on the
+    scenes of ``autofocus_scene.py`` (the reference's own recovery scene and
+    a cluttered one), and ``autofocus.pick_targets`` (:19-34) on a seeded
+    polar image.  matplotlib is absent here, so an empty module stands in
+    for it (autofocus.py only plots in ``main``).
+
+``python tests/golden/make_golden.py /path/to/bp_project autofocus`` rebuilds
+only the named fixtures.
 """
 from __future__ import annotations
 
@@ -231,13 +240,58 @@ def plans_case(gb):
     return out
 
 
+def import_autofocus():
+    mpl = types.ModuleType("matplotlib")
+    mpl.use = lambda *a, **k: None
+    plt = types.ModuleType("matplotlib.pyplot")
+    mpl.pyplot = plt
+    sys.modules.setdefault("matplotlib", mpl)
+    sys.modules.setdefault("matplotlib.pyplot", plt)
+    import autofocus  # noqa: E402
+    return autofocus
+
+
+def autofocus_case():
+    sys.path.insert(0, str(HERE))
+    import autofocus_scene as scene
+    af = import_autofocus()
+    out = {}
+    for name in ("recovery", "cluttered"):
+        s = getattr(scene, name)()
+        delta, stats = af.estimate_update(s.data, s.pos, s.points, s.r_start, s.dr, s.k, s.prf, s.cutoff)
+        before = float(np.sqrt(np.mean(s.err[:, :2] ** 2)))
+        after = float(np.sqrt(np.mean((s.err + delta)[:, :2] ** 2)))
+        out.update({f"{name}_delta": delta, f"{name}_coherence": stats["median_gradient_coherence"],
+                    f"{name}_rmse": np.array([before, after]), f"{name}_data_probe": s.data[::97, ::31]})
+        print(f"autofocus {name}: rmse {before:.4f} -> {after:.4f}, coherence "
+              f"{stats['median_gradient_coherence']:.4f}", flush=True)
+    p = scene.picks()
+    result = types.SimpleNamespace(image=p.image, origin=p.origin, side=p.side,
+                                   r=p.r0 + p.dr * np.arange(p.image.shape[0]),
+                                   u=p.u0 + p.du * np.arange(p.image.shape[1]))
+    for tiles in ((12, 12), (7, 5)):
+        pts, powers = af.pick_targets(result, *tiles)
+        out[f"picks_{tiles[0]}x{tiles[1]}_points"] = pts
+        out[f"picks_{tiles[0]}x{tiles[1]}_powers"] = powers
+        print(f"pick_targets {tiles}: {len(pts)} targets", flush=True)
+    return out
+
+
+CASES = {
+    "operator_validation": lambda ffbp, gb: operator_validation(ffbp, gb),
+    "points": lambda ffbp, gb: points_case(ffbp),
+    "kernels": lambda ffbp, gb: kernels_case(ffbp),
+    "plans": lambda ffbp, gb: plans_case(gb),
+    "autofocus": lambda ffbp, gb: autofocus_case(),
+}
+
+
 def main():
     root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    names = sys.argv[2:] or list(CASES)
     ffbp, gb = import_reference(root)
-    np.savez_compressed(HERE / "operator_validation.npz", **operator_validation(ffbp, gb))
-    np.savez_compressed(HERE / "points.npz", **points_case(ffbp))
-    np.savez_compressed(HERE / "kernels.npz", **kernels_case(ffbp))
-    np.savez_compressed(HERE / "plans.npz", **plans_case(gb))
+    for name in names:
+        np.savez_compressed(HERE / f"{name}.npz", **CASES[name](ffbp, gb))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,110 @@
+"""GPU autofocus against the reference's own outputs (tests/golden/autofocus.npz).
+
+Tolerances: sosfiltfilt kernel vs scipy <= 1e-12 relative (FP64 recursion,
+complex64 odd extension); estimate_update deltas within 1e-4 of the largest
+reference correction (the target contributions are computed in FP32 on the
+GPU, complex64 in the reference); pick_targets points identical and powers
+within 1e-6 (|z| of complex64 on the GPU vs numpy).
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+import autofocus_scene as scene  # noqa: E402
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from bp_project_gb300 import build
+    build.build()
+    from bp_project_gb300 import _native
+    _native.load()
+    return _native
+
+
+def _rel_max(est, ref):
+    est, ref = np.asarray(est), np.asarray(ref)
+    return float(np.abs(est - ref).max() / np.abs(ref).max())
+
+
+@pytest.mark.parametrize("shape,cutoff,fs", [((7, 300), 12.0, 1000.0), ((144, 2048), 1.0, 1000.0), ((1, 16), 50, 400)])
+def test_sosfiltfilt_matches_scipy(lib, shape, cutoff, fs):
+    from scipy import signal
+    from bp_project_gb300.autofocus import butter_lowpass, sosfiltfilt
+    rng = np.random.default_rng(sum(shape))
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    f = butter_lowpass(cutoff, fs)
+    ref = signal.sosfiltfilt(f.sos, x, axis=1)
+    est = sosfiltfilt(torch.from_numpy(x).cuda(), f).cpu().numpy()
+    assert est.dtype == np.complex128
+    err = _rel_max(est, ref)
+    print(f"sosfiltfilt {shape}: {err:.2e}")
+    assert err <= 1e-12
+
+
+def test_sosfiltfilt_rejects_short_rows(lib):
+    from bp_project_gb300.autofocus import butter_lowpass, sosfiltfilt
+    with pytest.raises(ValueError, match="padlen"):
+        sosfiltfilt(torch.zeros((2, 15), dtype=torch.complex64, device="cuda"), butter_lowpass(12.0, 1000.0))
+
+
+@pytest.mark.parametrize("name", ["recovery", "cluttered"])
+def test_estimate_update_matches_reference(golden, lib, name):
+    from bp_project_gb300.autofocus import estimate_update
+    g = golden("autofocus")
+    s = getattr(scene, name)()
+    delta, stats = estimate_update(torch.from_numpy(s.data).cuda(), torch.from_numpy(s.pos).cuda(),
+                                   torch.from_numpy(s.points).cuda(), s.r_start, s.dr, s.k, s.prf, s.cutoff)
+    delta = delta.cpu().numpy()
+    err = _rel_max(delta, g[f"{name}_delta"])
+    print(f"estimate_update {name}: {err:.2e}, coherence {stats['median_gradient_coherence']:.6f}")
+    assert err <= 1e-4
+    assert abs(stats["median_gradient_coherence"] - float(g[f"{name}_coherence"])) < 1e-5
+    if name == "recovery":  # validate_autofocus.py:20
+        before = np.sqrt(np.mean(s.err[:, :2] ** 2))
+        assert np.sqrt(np.mean((s.err + delta)[:, :2] ** 2)) < 0.35 * before
+
+
+@pytest.mark.parametrize("tiles", [(12, 12), (7, 5)])
+def test_pick_targets_matches_reference(golden, lib, tiles):
+    from bp_project_gb300.autofocus import pick_targets
+    from bp_project_gb300.ffbp import PolarImage
+    g = golden("autofocus")
+    p = scene.picks()
+    result = PolarImage(torch.from_numpy(p.image).cuda(), p.origin, p.r0, p.dr, p.u0, p.du, p.side)
+    pts, powers = pick_targets(result, *tiles)
+    key = f"picks_{tiles[0]}x{tiles[1]}"
+    np.testing.assert_allclose(pts.cpu().numpy(), g[key + "_points"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(powers.cpu().numpy(), g[key + "_powers"], rtol=1e-6)
+
+
+def test_entropy_autofocus_refocuses_injected_errors(lib):
+    """Config-3 geometry at 512 pulses x 128^2: the gradient autofocus brings the entropy of the
+    image formed on the perturbed track below the entropy of the image on the true track plus 1%."""
+    from bp_project_gb300 import scenes
+    from bp_project_gb300.autofocus import entropy_autofocus, image_entropy
+    from bp_project_gb300.autograd import backproject_lattice
+    cfg = scenes.scaled(scenes.CONFIGS["c3"], pulses=512, image_side=128)
+    sc = scenes.synthesize(cfg, device="cuda")
+    err, phase_err = scenes.inject_trajectory_error(sc)
+    lat = sc.lattice
+    geo = (tuple(lat.origin), tuple(lat.step_row), tuple(lat.step_col), lat.rows, lat.cols,
+           sc.range_start, sc.data_dr, sc.k)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a)).cuda()
+    data, w = dev(sc.data), dev(sc.weight)
+    truth = float(image_entropy(backproject_lattice(data, dev(sc.position), w, dev(sc.phase), *geo)))
+    pos, phase = dev(sc.position + err), dev(sc.phase + phase_err)
+    start = float(image_entropy(backproject_lattice(data, pos, w, phase, *geo)))
+    res = entropy_autofocus(data, pos, w, phase, *geo, steps=60)
+    print(f"entropy: truth {truth:.4f}, perturbed {start:.4f}, autofocus {res.entropy:.4f} "
+          f"after {res.evaluations} evaluations, {res.history[-1][0]:.2f} s")
+    assert start > truth + 0.5
+    assert res.entropy < truth * 1.01
