@@ -39,6 +39,12 @@ autofocus.npz
     polar image.  matplotlib is absent here, so an empty module stands in
     for it (autofocus.py only plots in ``main``).
 
+metrics.npz
+    ``sar_quality/metrics.py`` (focus_metrics, fidelity, impulse_metrics) on
+    seeded images and impulse cuts.  numpy 2 removed ``trapz``; the
+    generator aliases it to ``numpy.trapezoid`` (same trapezoidal rule)
+    before importing the module.
+
 ``python tests/golden/make_golden.py /path/to/bp_project autofocus`` rebuilds
 only the named fixtures.
 """
@@ -277,18 +283,60 @@ def autofocus_case():
     return out
 
 
+def metrics_cases():
+    """Seeded inputs of the metrics golden case (rebuilt by the tests)."""
+    rng = np.random.default_rng(515)
+    img = (0.02 * (rng.standard_normal((96, 80)) + 1j * rng.standard_normal((96, 80)))).astype(np.complex64)
+    img[40, 33] += 3.0
+    img[10:14, 60:63] += 0.7j
+    est = (img + 0.01 * (rng.standard_normal(img.shape) + 1j * rng.standard_normal(img.shape))
+           * np.exp(0.05j)).astype(np.complex64)
+    cuts = []
+    for shift, width, window in ((0.0, 1.0, False), (0.37, 1.3, True), (-0.21, 0.8, False)):
+        x = np.linspace(-12, 12, 481)
+        z = np.sinc((x - shift) / width).astype(np.complex128)
+        if window:
+            z = z * (0.54 + 0.46 * np.cos(np.pi * np.clip((x - shift) / 12, -1, 1)))
+        z = z + 1e-4 * (rng.standard_normal(x.size) + 1j * rng.standard_normal(x.size))
+        cuts.append((x, z))
+    return img, est, cuts
+
+
+def metrics_case(root):
+    np.trapz = np.trapezoid  # removed in numpy 2; the reference calls it
+    sys.path.insert(0, str(root / "sar_quality"))
+    import metrics as ref  # noqa: E402
+    img, est, cuts = metrics_cases()
+    out = {}
+    fm = ref.focus_metrics(img)
+    out["focus"] = np.array([fm["entropy_nats"], fm["normalized_entropy"], fm["intensity_contrast"],
+                             fm["amplitude_contrast"], fm["brightest_1pct_energy_fraction"]])
+    fd = ref.fidelity(img, est)
+    out["fidelity"] = np.array([fd["relative_complex_error"], fd["ser_db"], fd["complex_coherence"],
+                                fd["phase_bias_deg"], fd["phase_std_deg_above_minus30db"], fd["phase_mask_samples"]])
+    for i, (x, z) in enumerate(cuts):
+        m = ref.impulse_metrics(x, z)
+        out[f"impulse{i}"] = np.array([m["irw_m"], m["peak_offset_m"], m["pslr_db"], m["islr_db"],
+                                       *m["mainlobe_bounds_m"], *m["mainlobe_minima_db"]])
+        print(f"impulse {i}: irw {m['irw_m']:.4f} pslr {m['pslr_db']:.2f} islr {m['islr_db']:.2f}", flush=True)
+    return out
+
+
 CASES = {
     "operator_validation": lambda ffbp, gb: operator_validation(ffbp, gb),
     "points": lambda ffbp, gb: points_case(ffbp),
     "kernels": lambda ffbp, gb: kernels_case(ffbp),
     "plans": lambda ffbp, gb: plans_case(gb),
     "autofocus": lambda ffbp, gb: autofocus_case(),
+    "metrics": lambda ffbp, gb: metrics_case(ROOT_ARG[0]),
 }
+ROOT_ARG = [Path("/root/reference")]
 
 
 def main():
     root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     names = sys.argv[2:] or list(CASES)
+    ROOT_ARG[0] = root
     ffbp, gb = import_reference(root)
     for name in names:
         np.savez_compressed(HERE / f"{name}.npz", **CASES[name](ffbp, gb))
