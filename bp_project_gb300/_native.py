@@ -51,6 +51,19 @@ class FFBPNode(ctypes.Structure):
                 ("side", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class BatchScene(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("pulses", ctypes.c_int32), ("samples", ctypes.c_int32),
+                ("pos", ctypes.c_void_p), ("weight", ctypes.c_void_p), ("phase", ctypes.c_void_p),
+                ("range_start", ctypes.c_double), ("data_dr", ctypes.c_double), ("k", ctypes.c_double),
+                ("kind", ctypes.c_int32), ("lattice", Lattice), ("nodes", ctypes.POINTER(FFBPNode)),
+                ("n_nodes", ctypes.c_int32), ("crop_r0", ctypes.c_int32), ("crop_u0", ctypes.c_int32),
+                ("crop_nr", ctypes.c_int32), ("crop_nu", ctypes.c_int32), ("tile_lc", ctypes.c_int32),
+                ("chunk_pulses", ctypes.c_int32), ("out", ctypes.c_void_p)]
+
+
+BATCH_DIRECT = 0
+BATCH_FFBP = 1
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -78,6 +91,14 @@ SIGNATURES = {
     "sarbp_backproject_lattice_adjoint_workspace": ([ctypes.POINTER(Lattice), _I], _Z),
     "sarbp_backproject_lattice_adjoint": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(Lattice), _D, _D, _D, _P, _P, _P, _P,
                                            _P, _Z, _P], _I),
+    "sarbp_batch_create": ([ctypes.POINTER(BatchScene), _I, _I, ctypes.POINTER(_P)], _I),
+    "sarbp_batch_destroy": ([_P], None),
+    "sarbp_batch_workspace_bytes": ([_P], _Z),
+    "sarbp_batch_launch_count": ([_P], _I),
+    "sarbp_batch_info": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                          ctypes.POINTER(_D)], _I),
+    "sarbp_batch_bind": ([_P, _P, _Z, _P], _I),
+    "sarbp_batch_execute": ([_P, _P], _I),
     "sarbp_sosfiltfilt_workspace": ([_I, _I, _I], _Z),
     "sarbp_sosfiltfilt": ([_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _Z, _P], _I),
     "sarbp_regrid": ([_P, ctypes.POINTER(PolarGrid), ctypes.POINTER(PolarGrid), _D, _I, _P, _P], _I),

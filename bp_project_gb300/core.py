@@ -227,6 +227,23 @@ def cast_c128_to_c64(t, out=None):
     return out
 
 
+def node_array(nodes):
+    """Pre-order NodePlan-like objects -> ctypes sarbp_ffbp_node array (children as indices)."""
+    arr = (nat.FFBPNode * len(nodes))()
+    index = {id(n): i for i, n in enumerate(nodes)}
+    for i, n in enumerate(nodes):
+        e = arr[i]
+        e.origin[:] = [float(v) for v in n.origin]
+        e.r0, e.dr, e.u0, e.du = float(n.r0), float(n.dr), float(n.u0), float(n.du)
+        e.nr, e.nu, e.side = int(n.nr), int(n.nu), int(n.side)
+        e.a, e.b = int(n.a), int(n.b)
+        left = getattr(n, "left", None)
+        right = getattr(n, "right", None)
+        e.left = -1 if left is None else (left if isinstance(left, int) else index[id(left)])
+        e.right = -1 if right is None else (right if isinstance(right, int) else index[id(right)])
+    return arr
+
+
 class FFBPProgram:
     """Level-batched FFBP over a node tree (one launch for the leaves, one per height).
 
@@ -238,18 +255,7 @@ class FFBPProgram:
 
     def __init__(self, nodes, crop_r, crop_u, mode=DEFAULT_MODE, device="cuda"):
         self.mode = mode
-        arr = (nat.FFBPNode * len(nodes))()
-        index = {id(n): i for i, n in enumerate(nodes)}
-        for i, n in enumerate(nodes):
-            e = arr[i]
-            e.origin[:] = [float(v) for v in n.origin]
-            e.r0, e.dr, e.u0, e.du = float(n.r0), float(n.dr), float(n.u0), float(n.du)
-            e.nr, e.nu, e.side = int(n.nr), int(n.nu), int(n.side)
-            e.a, e.b = int(n.a), int(n.b)
-            left = getattr(n, "left", None)
-            right = getattr(n, "right", None)
-            e.left = -1 if left is None else (left if isinstance(left, int) else index[id(left)])
-            e.right = -1 if right is None else (right if isinstance(right, int) else index[id(right)])
+        arr = node_array(nodes)
         self.crop = (int(crop_r[0]), int(crop_u[0]), int(crop_r[1] - crop_r[0]), int(crop_u[1] - crop_u[0]))
         handle = ctypes.c_void_p()
         lib = nat.load()

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "plan.cuh"
 
 namespace sarbp {
 
@@ -107,6 +108,12 @@ PulseInputs inputs_of(const float* data, int pulses, int samples, const double* 
     return in;
 }
 
+
+// Envelope assumed for point tiles: tiles wider than this run through the FP64 fallback.
+constexpr double kPointRadius = 24.0;
+
+}  // namespace
+
 double lattice_radius(const sarbp_lattice& lat, int lc) {
     const double hr = (double)((kSplitTilePixels >> lc) >> 1), hc = (double)((1 << lc) >> 1);
     double s = 0.0;
@@ -117,39 +124,11 @@ double lattice_radius(const sarbp_lattice& lat, int lc) {
     return sqrt(s) * 1.0001 + 1e-6;
 }
 
-// Envelope assumed for point tiles: tiles wider than this run through the FP64 fallback.
-constexpr double kPointRadius = 24.0;
-
-}  // namespace
 }  // namespace sarbp
 
 using namespace sarbp;
 
 // ---- FFBP plan object -------------------------------------------------------------------
-struct sarbp_ffbp_plan {
-    int mode = SARBP_SPLIT;
-    int n_nodes = 0;
-    std::vector<PolarDesc> nodes;
-    std::vector<int> height;
-    int max_height = 0;
-    // Split: tile items; plain: 256-pixel blocks.  Stage h occupies [stage_begin[h], +stage_count[h]).
-    std::vector<TileItem> items;
-    std::vector<int2> blocks;
-    std::vector<int> stage_begin, stage_count;
-    int leaf_chunk = 1, leaf_wb = 4;
-    long long table_entries = 0;  // split: float4 row/column geometry entries of all nodes
-    int max_dim = 1;
-    std::vector<int> leaves;      // split: leaf node indices
-    int max_pulse = 0;            // split: largest pulse index + 1 used by a leaf
-    int leaf_span_bins = 4;       // split: range bins a 32-row leaf tile spans (before the pulse offsets)
-    long long merge_items = 0;    // split: tile items of all merge levels (contiguous after the leaves)
-    size_t node_bytes = 0, work_bytes = 0, leaf_list_bytes = 0, table_bytes = 0, table_offset = 0,
-           prec_offset = 0, prec_bytes = 0, crec_offset = 0, crec_bytes = 0, arena_offset = 0, arena_bytes = 0,
-           total_bytes = 0;
-    void* bound = nullptr;
-    size_t bound_bytes = 0;
-    int launches = 0;
-};
 
 extern "C" {
 

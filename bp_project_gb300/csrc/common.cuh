@@ -95,6 +95,7 @@ struct PolarDesc {
     int pad;
     long long rows_off;                  // FFBP: first entry of this node's row table (float4 (g_hi, g_lo, psi, 0))
     long long cols_off;                  // FFBP: first entry of this node's column table (float4 (c_hi, c_lo, u_hi, u_lo))
+    float2* dst;                         // if set: where the node's window is written (batched scene roots)
 };
 
 struct TileItem {
@@ -147,6 +148,8 @@ constexpr int kSplitThreads = 256;
 constexpr int kSplitTilePixels = 1024;  // 256 threads x 4 pixels
 // Bins each pulse window needs for tiles of at most `radius` metres (pixel offset from the tile centre).
 int split_window_bins(double radius, double data_dr);
+// Radius (m) of a lattice tile of 1024 >> lc rows by 1 << lc columns about its centre pixel.
+double lattice_radius(const sarbp_lattice& lat, int lc);
 // Pulses per shared-memory chunk that fit `window_bins` within the shared-memory budget.
 int split_chunk_for(int window_bins, int requested);
 // Tile column exponent (2..5) that makes a polar tile of grid g closest to square in metres,
@@ -164,6 +167,31 @@ size_t split_adjoint_workspace(const sarbp_lattice& lat, int pulses);
 int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat, int chunk, int window_bins,
                                  const float2* grad, float* partials, double* grad_pos, double* grad_phase,
                                  double* grad_weight, cudaStream_t s);
+
+// Batched scenes (persistent work-queue kernels).  One descriptor per scene.
+struct BatchSceneDesc {
+    PulseInputs in;
+    int kind;               // 0 direct lattice, 1 FFBP
+    sarbp_lattice lat;      // direct scenes
+    int lc;                 // direct: log2 of tile columns (2..5)
+    int chunk;              // pulses per staged chunk
+    int window_bins;        // range bins per pulse window
+    float2* out;            // direct output image
+    long long prec_offset;  // FFBP: first pulse record of the scene
+};
+size_t split_batch_scene_bytes();
+// Writes the device form of `d` to dst; returns the dynamic shared memory its tiles need.
+size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst);
+int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm);
+int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int n_nodes, int max_dim,
+                                const int* leaves, int n_leaves, const TileItem* merge_items, int n_merge_items,
+                                float4* tables, void* precs, void* crecs, float2* arena, cudaStream_t s);
+int launch_split_batch_bp(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                          const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
+                          size_t smem, cudaStream_t s);
+int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                              const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
+                              cudaStream_t s);
 
 // Zero-phase IIR smoothing along rows (autofocus phase-history filter).
 size_t sosfiltfilt_workspace(int rows, int n, int padlen);

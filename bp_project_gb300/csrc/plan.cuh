@@ -1,0 +1,32 @@
+// Host-side FFBP plan object (shared by the single-scene plan entry points and the
+// scene batch, which reuses plans built by sarbp_ffbp_plan_create).
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+struct sarbp_ffbp_plan {
+    int mode = SARBP_SPLIT;
+    int n_nodes = 0;
+    std::vector<sarbp::PolarDesc> nodes;
+    std::vector<int> height;
+    int max_height = 0;
+    // Split: tile items; plain: 256-pixel blocks.  Stage h occupies [stage_begin[h], +stage_count[h]).
+    std::vector<sarbp::TileItem> items;
+    std::vector<int2> blocks;
+    std::vector<int> stage_begin, stage_count;
+    int leaf_chunk = 1, leaf_wb = 4;
+    long long table_entries = 0;  // split: float4 row/column geometry entries of all nodes
+    int max_dim = 1;
+    std::vector<int> leaves;      // split: leaf node indices
+    int max_pulse = 0;            // split: largest pulse index + 1 used by a leaf
+    int leaf_span_bins = 4;       // split: range bins a 32-row leaf tile spans (before the pulse offsets)
+    long long merge_items = 0;    // split: tile items of all merge levels (contiguous after the leaves)
+    size_t node_bytes = 0, work_bytes = 0, leaf_list_bytes = 0, table_bytes = 0, table_offset = 0,
+           prec_offset = 0, prec_bytes = 0, crec_offset = 0, crec_bytes = 0, arena_offset = 0, arena_bytes = 0,
+           total_bytes = 0;
+    void* bound = nullptr;
+    size_t bound_bytes = 0;
+    int launches = 0;
+};

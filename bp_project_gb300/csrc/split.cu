@@ -868,19 +868,32 @@ __global__ void __launch_bounds__(kThreads, 3) split_polar_kernel(SplitParams P,
     store_window(J, g.win_nr, g.win_nu, px, P.out + blockIdx.y * P.split_stride, P.out_stride);
 }
 
+// One lattice tile over pulses [p0, p1): the per-item body shared by the one-tile-per-CTA
+// kernel and the persistent batch kernel.
+template <bool HAS_Z>
+__device__ __forceinline__ void lattice_tile(const SplitParams& P, const sarbp_lattice& lat, int lc, int tile_r,
+                                             int tile_u, int p0, int p1, float2* out, TileShared& S, char* smem) {
+    Job J;
+    J.lat = lat;
+    J.lc = lc;
+    J.tile_r = tile_r;
+    J.tile_u = tile_u;
+    J.p0 = p0;
+    J.p1 = p1;
+    Pix px[kPX];
+    setup_lattice<HAS_Z>(J, S, px);
+    pulse_loop<HAS_Z, false>(P, J, S, smem, px);
+    store_window(J, lat.rows, lat.cols, px, out, lat.cols);
+}
+
 template <bool HAS_Z>
 __global__ void __launch_bounds__(kThreads, 3) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    Job J;
-    J.lat = lat;
-    J.lc = lc;
-    tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
-    split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, J.p0, J.p1);
-    Pix px[kPX];
-    setup_lattice<HAS_Z>(J, S, px);
-    pulse_loop<HAS_Z, false>(P, J, S, smem, px);
-    store_window(J, lat.rows, lat.cols, px, P.out + blockIdx.y * P.split_stride, lat.cols);
+    int tile_r, tile_u, p0, p1;
+    tile_of(blockIdx.x, lat.cols, lc, tile_r, tile_u);
+    split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, p0, p1);
+    lattice_tile<HAS_Z>(P, lat, lc, tile_r, tile_u, p0, p1, P.out + blockIdx.y * P.split_stride, S, smem);
 }
 
 __global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P, const double* __restrict__ xyz,
@@ -960,10 +973,8 @@ __global__ void adjoint_sum_kernel(const float* __restrict__ partials, int ntile
 }
 
 // ---- FFBP: per-node tables and per-pulse leaf records (prologue kernels) ------------------
-__global__ void ffbp_tables_kernel(double K, double range_start, double inv_dr, const PolarDesc* __restrict__ nodes,
-                                   float4* __restrict__ tables) {
-    const PolarDesc& g = nodes[blockIdx.y];
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void table_entries(double K, double range_start, double inv_dr, const PolarDesc& g, int t,
+                                              float4* __restrict__ tables) {
     if (t < g.nr) {
         const double r = g.r0 + (double)t * g.dr;
         const double gg = sqrt(fmax(0.0, r * r - g.oz * g.oz));
@@ -986,6 +997,11 @@ __global__ void ffbp_tables_kernel(double K, double range_start, double inv_dr, 
     }
 }
 
+__global__ void ffbp_tables_kernel(double K, double range_start, double inv_dr, const PolarDesc* __restrict__ nodes,
+                                   float4* __restrict__ tables) {
+    table_entries(K, range_start, inv_dr, nodes[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x, tables);
+}
+
 // Leaf pulses relative to the leaf's phase centre O (origin formulation).
 // A = -K (pos - O) is split into a multiple of a per-leaf power-of-two
 // quantum with <= 10 significant bits plus an FP32 remainder.
@@ -995,11 +1011,9 @@ struct PulseRec {
     float4 c;  // (pos - O).x, .y, .z, weight
 };
 
-__global__ void ffbp_leaf_pulses_kernel(double K, const double* __restrict__ pos, const double* __restrict__ weight,
-                                        const double* __restrict__ phase, const PolarDesc* __restrict__ nodes,
-                                        const int* __restrict__ leaves, PulseRec* __restrict__ recs) {
-    __shared__ int amax;
-    const PolarDesc& g = nodes[leaves[blockIdx.x]];
+__device__ __forceinline__ void leaf_pulses(double K, const double* __restrict__ pos, const double* __restrict__ weight,
+                                            const double* __restrict__ phase, const PolarDesc& g,
+                                            PulseRec* __restrict__ recs, int& amax) {
     if (threadIdx.x == 0) amax = 0;
     __syncthreads();
     float m = 0.0f;
@@ -1024,6 +1038,13 @@ __global__ void ffbp_leaf_pulses_kernel(double K, const double* __restrict__ pos
         r.c = make_float4((float)ax, (float)ay, (float)az, (float)weight[n]);
         recs[n] = r;
     }
+}
+
+__global__ void ffbp_leaf_pulses_kernel(double K, const double* __restrict__ pos, const double* __restrict__ weight,
+                                        const double* __restrict__ phase, const PolarDesc* __restrict__ nodes,
+                                        const int* __restrict__ leaves, PulseRec* __restrict__ recs) {
+    __shared__ int amax;
+    leaf_pulses(K, pos, weight, phase, nodes[leaves[blockIdx.x]], recs, amax);
 }
 
 // ---- FFBP: leaves (origin formulation) ---------------------------------------------------
@@ -1056,17 +1077,12 @@ __device__ __forceinline__ void unit_pair(float p, float e, float& h, float& l, 
     full = p + e;
 }
 
-__global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
-                                                                 const TileItem* __restrict__ items,
-                                                                 const float4* __restrict__ tables,
-                                                                 const PulseRec* __restrict__ precs,
-                                                                 float2* __restrict__ arena, float2* root_out,
-                                                                 int root) {
-    extern __shared__ __align__(16) char smem[];
-    __shared__ int s_base[kMaxChunk];
-    __shared__ float s_wt[kMaxChunk];
-    __shared__ int s_nfit;
-    const TileItem it = items[blockIdx.x];
+// One leaf tile: the per-item body of the leaf kernels.  precs holds the pulse records of
+// the leaf's scene (indexed by pulse); a node with a destination pointer writes there.
+__device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc* __restrict__ nodes, const TileItem it,
+                                          const float4* __restrict__ tables, const PulseRec* __restrict__ precs,
+                                          float2* __restrict__ arena, float2* root_out, int root, char* smem,
+                                          int* s_base, float* s_wt, int& s_nfit) {
     const PolarDesc g = nodes[it.node];
     const int lc = g.tile_lc, cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1216,13 +1232,26 @@ __global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, 
         }
         c0 += chn;
     }
-    float2* dst = it.node == root ? root_out : arena + g.out_offset;
+    float2* dst = g.dst ? g.dst : (it.node == root ? root_out : arena + g.out_offset);
 #pragma unroll
     for (int k = 0; k < kPX; ++k) {
         const int p = tid + kThreads * k;
         const int wr = it.tile_r + (p >> lc), wu = it.tile_u + (p & (cols_t - 1));
         if (wr < g.win_nr && wu < g.win_nu) dst[(long long)wr * g.out_stride + wu] = make_float2(px[k].ar, px[k].ai);
     }
+}
+
+__global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+                                                                 const TileItem* __restrict__ items,
+                                                                 const float4* __restrict__ tables,
+                                                                 const PulseRec* __restrict__ precs,
+                                                                 float2* __restrict__ arena, float2* root_out,
+                                                                 int root) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ int s_base[kMaxChunk];
+    __shared__ float s_wt[kMaxChunk];
+    __shared__ int s_nfit;
+    leaf_tile(P, nodes, items[blockIdx.x], tables, precs, arena, root_out, root, smem, s_base, s_wt, s_nfit);
 }
 
 // ---- FFBP: merges (both child regrids of one parent tile) --------------------------------
@@ -1238,12 +1267,9 @@ struct ChildRec {
 
 // One thread per (merge tile, child): the tile centre is the FP64 position of
 // the tile's centre pixel, the same point setup_polar_tab measures offsets from.
-__global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_scale_w,
-                                          const PolarDesc* __restrict__ nodes, const TileItem* __restrict__ items,
-                                          int n_items, float2* __restrict__ arena, ChildRec* __restrict__ out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * n_items) return;
-    const TileItem it = items[t >> 1];
+__device__ __forceinline__ void child_record(double K, double scale_w, double inv_scale_w,
+                                             const PolarDesc* __restrict__ nodes, const TileItem it, int t,
+                                             float2* __restrict__ arena, ChildRec* __restrict__ out) {
     const PolarDesc& g = nodes[it.node];
     const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
     const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
@@ -1281,7 +1307,15 @@ __global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_s
     out[t] = R;
 }
 
-__device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildRec& R, const Pix& q) {
+__global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_scale_w,
+                                          const PolarDesc* __restrict__ nodes, const TileItem* __restrict__ items,
+                                          int n_items, float2* __restrict__ arena, ChildRec* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * n_items) return;
+    child_record(K, scale_w, inv_scale_w, nodes, items[t >> 1], t, arena, out);
+}
+
+__device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const Pix& q) {
     const float L = fmaf(R.b.x, q.dx, R.b.y * q.dy);
     const float q2 = fmaf(-L, L, q.d2);
     const float B = rcp_approx(fmaf(2.0f, L, R.b.z));
@@ -1324,7 +1358,7 @@ __device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildR
         }
     }
     const float tb = fmaf(R.a.x, q.dxh, R.a.y * q.dyh);
-    float sm = fmaf(P.Kf, eps, R.c.x);
+    float sm = fmaf(Kf, eps, R.c.x);
     sm = fmaf(R.a.x, q.dxl, sm);
     sm = fmaf(R.a.y, q.dyl, sm);
     sm = fmaf(R.a.z, q.dx, sm);
@@ -1336,6 +1370,32 @@ __device__ __forceinline__ float2 child_value(const SplitParams& P, const ChildR
     return make_float2(vr * cs - vi * sn, vr * sn + vi * cs);
 }
 
+// One merge tile: both children regridded onto the parent tile, each rounded to complex64,
+// then added (the reference's rounding points).  crec points at the tile's two child records.
+__device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
+                                           const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
+                                           ChildRec* C, float2* __restrict__ arena, float2* root_out, int root,
+                                           TileShared& S, char* smem) {
+    Job J;
+    J.g = nodes[it.node];
+    J.lc = J.g.tile_lc;
+    J.tile_r = it.tile_r;
+    J.tile_u = it.tile_u;
+    if (threadIdx.x < 2) C[threadIdx.x] = crec[threadIdx.x];
+    Pix px[kPX];
+    TabF& T = *reinterpret_cast<TabF*>(smem);
+    setup_polar_tab(J, S, T, tables, px);
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const float2 a = child_value(Kf, C[0], px[k]);
+        const float2 b = child_value(Kf, C[1], px[k]);
+        px[k].ar = __fadd_rn(a.x, b.x);
+        px[k].ai = __fadd_rn(a.y, b.y);
+    }
+    float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
+    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+}
+
 __global__ void __launch_bounds__(kThreads, 3) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
                                                                   const float4* __restrict__ tables,
@@ -1345,25 +1405,8 @@ __global__ void __launch_bounds__(kThreads, 3) split_merge_kernel(SplitParams P,
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     __shared__ ChildRec C[2];
-    const TileItem it = items[blockIdx.x];
-    Job J;
-    J.g = nodes[it.node];
-    J.lc = J.g.tile_lc;
-    J.tile_r = it.tile_r;
-    J.tile_u = it.tile_u;
-    if (threadIdx.x < 2) C[threadIdx.x] = crecs[2 * (long long)blockIdx.x + threadIdx.x];
-    Pix px[kPX];
-    TabF& T = *reinterpret_cast<TabF*>(smem);
-    setup_polar_tab(J, S, T, tables, px);
-#pragma unroll
-    for (int k = 0; k < kPX; ++k) {
-        const float2 a = child_value(P, C[0], px[k]);
-        const float2 b = child_value(P, C[1], px[k]);
-        px[k].ar = __fadd_rn(a.x, b.x);
-        px[k].ai = __fadd_rn(a.y, b.y);
-    }
-    float2* dst = it.node == root ? root_out : arena + J.g.out_offset;
-    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+    merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, S,
+               smem);
 }
 
 SplitParams make_params(const PulseInputs& in, int chunk, int cap, int pulse_split) {
@@ -1590,6 +1633,188 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
                                                       arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_merges");
+}
+
+// ---- batched scenes: persistent work-queue kernels ------------------------------------------
+//
+// Many independent scenes (direct lattice images and FFBP trees) run as one work list.
+// Each scene's parameters live in a device array; tile items carry their scene in
+// TileItem::pad and FFBP nodes in PolarDesc::pad.  The BP kernel is persistent: every
+// CTA takes the next item from a global counter until the list is exhausted, so scenes
+// of very different sizes share the GPU without per-scene launches or idle tails.  Items
+// are independent (no item waits for another), so the persistent grid needs no
+// co-residency guarantee.  Merge levels run as one persistent launch per tree height
+// over the nodes of that height in every FFBP scene.
+namespace {
+
+struct BatchScene {
+    SplitParams P;          // pulse inputs, constants, chunk / window capacity; P.out = direct output
+    sarbp_lattice lat;      // direct scenes
+    int kind;               // 0 direct lattice, 1 FFBP
+    int lc;                 // direct: log2 of tile columns
+    int has_z;
+    int pad;
+    long long prec_offset;  // FFBP: first pulse record of the scene
+};
+
+__device__ __forceinline__ int next_item(int* counter, int& s_item) {
+    __syncthreads();  // every thread is done with the previous item's shared state
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    return s_item;
+}
+
+__device__ __forceinline__ void load_scene(const BatchScene* __restrict__ scenes, int scene, BatchScene& sc) {
+    const int* src = reinterpret_cast<const int*>(scenes + scene);
+    int* dst = reinterpret_cast<int*>(&sc);
+    for (int w = threadIdx.x; w < (int)(sizeof(BatchScene) / sizeof(int)); w += kThreads) dst[w] = src[w];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads, 3) batch_bp_kernel(const BatchScene* __restrict__ scenes,
+                                                               const PolarDesc* __restrict__ nodes,
+                                                               const TileItem* __restrict__ items, int nitems,
+                                                               const float4* __restrict__ tables,
+                                                               const PulseRec* __restrict__ precs,
+                                                               float2* __restrict__ arena, int* counter) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    __shared__ int s_base[kMaxChunk];
+    __shared__ float s_wt[kMaxChunk];
+    __shared__ int s_nfit, s_item, s_scene;
+    __shared__ __align__(16) BatchScene sc;
+    if (threadIdx.x == 0) s_scene = -1;
+    for (;;) {
+        const int idx = next_item(counter, s_item);
+        if (idx >= nitems) return;
+        const TileItem it = items[idx];
+        if (it.pad != s_scene) {  // uniform across the block
+            load_scene(scenes, it.pad, sc);
+            if (threadIdx.x == 0) s_scene = it.pad;
+        }
+        if (sc.kind == 0)  // flat lattices only (checked when the batch is created)
+            lattice_tile<false>(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
+        else
+            leaf_tile(sc.P, nodes, it, tables, precs + sc.prec_offset, arena, nullptr, -1, smem, s_base, s_wt, s_nfit);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 3) batch_merge_kernel(const BatchScene* __restrict__ scenes,
+                                                                  const PolarDesc* __restrict__ nodes,
+                                                                  const TileItem* __restrict__ items, int nitems,
+                                                                  const float4* __restrict__ tables,
+                                                                  const ChildRec* __restrict__ crecs,
+                                                                  float2* __restrict__ arena, int* counter) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    __shared__ ChildRec C[2];
+    __shared__ int s_item;
+    for (;;) {
+        const int idx = next_item(counter, s_item);
+        if (idx >= nitems) return;
+        const TileItem it = items[idx];
+        merge_tile(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, nullptr, -1, S, smem);
+    }
+}
+
+__global__ void batch_tables_kernel(const BatchScene* __restrict__ scenes, const PolarDesc* __restrict__ nodes,
+                                    float4* __restrict__ tables) {
+    const PolarDesc& g = nodes[blockIdx.y];
+    const SplitParams& P = scenes[g.pad].P;
+    table_entries(P.K, P.in.range_start, P.inv_dr, g, blockIdx.x * blockDim.x + threadIdx.x, tables);
+}
+
+__global__ void batch_leaf_pulses_kernel(const BatchScene* __restrict__ scenes, const PolarDesc* __restrict__ nodes,
+                                         const int* __restrict__ leaves, PulseRec* __restrict__ recs) {
+    __shared__ int amax;
+    const PolarDesc& g = nodes[leaves[blockIdx.x]];
+    const BatchScene& sc = scenes[g.pad];
+    leaf_pulses(sc.P.K, sc.P.in.pos, sc.P.in.weight, sc.P.in.phase, g, recs + sc.prec_offset, amax);
+}
+
+__global__ void batch_child_records_kernel(const BatchScene* __restrict__ scenes, const PolarDesc* __restrict__ nodes,
+                                           const TileItem* __restrict__ items, int n_items, float2* __restrict__ arena,
+                                           ChildRec* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * n_items) return;
+    const TileItem it = items[t >> 1];
+    const SplitParams& P = scenes[it.pad].P;
+    child_record(P.K, P.scale_w, P.inv_scale_w, nodes, it, t, arena, out);
+}
+
+}  // namespace
+
+size_t split_batch_scene_bytes() { return sizeof(BatchScene); }
+
+size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
+    BatchScene b{};
+    b.P = make_params(d.in, d.chunk, capacity_for(d.chunk, d.window_bins), 1);
+    b.P.out = d.out;
+    b.lat = d.lat;
+    b.kind = d.kind;
+    b.lc = d.lc;
+    b.has_z = (d.lat.step_row[2] != 0.0 || d.lat.step_col[2] != 0.0) ? 1 : 0;
+    b.prec_offset = d.prec_offset;
+    memcpy(dst, &b, sizeof(b));
+    return (size_t)kMaxChunk * (d.kind == 0 ? sizeof(Rec) : sizeof(LeafRec)) + (size_t)b.P.cap * 32;
+}
+
+int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm) {
+    if (int st = prepare(batch_bp_kernel, smem)) return st;
+    if (int st = prepare(batch_merge_kernel, sizeof(TabF))) return st;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bp_blocks_per_sm, batch_bp_kernel, kThreads, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_blocks_per_sm, batch_merge_kernel, kThreads,
+                                                          sizeof(TabF));
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
+    return SARBP_OK;
+}
+
+int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int n_nodes, int max_dim,
+                                const int* leaves, int n_leaves, const TileItem* merge_items, int n_merge_items,
+                                float4* tables, void* precs, void* crecs, float2* arena, cudaStream_t s) {
+    const BatchScene* sc = reinterpret_cast<const BatchScene*>(scenes);
+    if (n_nodes > 0) {
+        dim3 grid((max_dim + kThreads - 1) / kThreads, n_nodes);
+        batch_tables_kernel<<<grid, kThreads, 0, s>>>(sc, nodes, tables);
+        note_launches(1);
+        if (int st = check_launch("batch_tables")) return st;
+    }
+    if (n_leaves > 0) {
+        batch_leaf_pulses_kernel<<<n_leaves, 128, 0, s>>>(sc, nodes, leaves, reinterpret_cast<PulseRec*>(precs));
+        note_launches(1);
+        if (int st = check_launch("batch_leaf_pulses")) return st;
+    }
+    if (n_merge_items > 0) {
+        batch_child_records_kernel<<<grid_blocks(2LL * n_merge_items, kThreads), kThreads, 0, s>>>(
+            sc, nodes, merge_items, n_merge_items, arena, reinterpret_cast<ChildRec*>(crecs));
+        note_launches(1);
+        if (int st = check_launch("batch_child_records")) return st;
+    }
+    return SARBP_OK;
+}
+
+int launch_split_batch_bp(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                          const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
+                          size_t smem, cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    if (int st = prepare(batch_bp_kernel, smem)) return st;
+    batch_bp_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes, items, nitems,
+                                                   tables, reinterpret_cast<const PulseRec*>(precs), arena, counter);
+    note_launches(1);
+    return check_launch("batch_bp");
+}
+
+int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                              const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
+                              cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    batch_merge_kernel<<<blocks, kThreads, sizeof(TabF), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
+                                                              items, nitems, tables,
+                                                              reinterpret_cast<const ChildRec*>(crecs), arena,
+                                                              counter);
+    note_launches(1);
+    return check_launch("batch_merges");
 }
 
 }  // namespace sarbp

@@ -115,6 +115,41 @@ CONFIGS = {
 }
 
 
+def batch_configs(count: int = 64, seed: int = 4096, pulse_choices=None, side_choices=(256, 512, 1024, 2048),
+                  near_range=(3.5e3, 8.0e3)):
+    """The uneven multi-scene workload: ``count`` scenes with the 1024-pulse scene's radar
+    (9.6 GHz, 150 MHz, 180 MHz sampling, 1 kHz PRF, 100 m/s, 3 km altitude) and
+
+    * pulses uniform over {512, 1024, ..., 8192},
+    * image side uniform over {256, 512, 1024, 2048} at 0.5 m,
+    * near slant range uniform in ``near_range`` (the lower end is 3.5 km, not 3 km:
+      at 3 km altitude a 3 km slant range is the nadir point, where ground range is 0),
+    * 4..16 seeded point targets (amplitude 1..10) over 256 clutter scatterers, no noise,
+    * half direct BP, half FFBP (leaves of 16 pulses), in seeded random order.
+
+    Range bins per scene cover the image from every pulse (rounded up to 256).
+    Returns a list of (SceneConfig, kind) with kind "direct" or "ffbp"."""
+    rng = np.random.default_rng(seed)
+    base = CONFIGS["c0"]
+    pulse_choices = np.arange(512, 8193, 512) if pulse_choices is None else np.asarray(pulse_choices)
+    kinds = rng.permutation(np.array(["direct", "ffbp"] * ((count + 1) // 2))[:count])
+    out = []
+    for i in range(count):
+        pulses = int(rng.choice(pulse_choices))
+        side = int(rng.choice(side_choices))
+        near = float(rng.uniform(*near_range))
+        cfg = replace(base, name=f"batch{i}", pulses=pulses, image_side=side, near_slant=near,
+                      n_targets=int(rng.integers(4, 17)), target_grid=False, target_amplitude=(1.0, 10.0),
+                      clutter_scatterers=256, clutter_sigma=0.1, snr_db=None, leaf_size=16,
+                      seed=int(rng.integers(1 << 30)))
+        half_ap = 0.5 * pulses * cfg.pulse_spacing
+        far_ground = cfg.near_ground + side * cfg.pixel_spacing
+        far = float(np.sqrt(far_ground**2 + (0.5 * side * cfg.pixel_spacing + half_ap) ** 2 + cfg.altitude**2))
+        samples = int(np.ceil(((far - cfg.range_start) / cfg.data_dr + 160) / 256.0) * 256)
+        out.append((replace(cfg, samples=samples), str(kinds[i])))
+    return out
+
+
 def scaled(config: SceneConfig, pulses: int | None = None, samples: int | None = None,
            image_side: int | None = None, **kw) -> SceneConfig:
     """A smaller scene with the same geometry (used for parity checks)."""

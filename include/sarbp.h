@@ -182,6 +182,52 @@ int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples
                                       double* grad_pos, double* grad_phase, double* grad_weight, void* workspace,
                                       size_t workspace_bytes, void* stream);
 
+/* ---- scene batches (persistent work-queue kernels) ------------------------- */
+
+/* Many independent scenes of uneven pulse and pixel counts formed together:
+ * direct split-precision BP onto a flat lattice, or split-precision FFBP of a
+ * plan (the nodes sarbp_ffbp_plan_create takes).  All scenes' direct tiles and
+ * FFBP leaf tiles run in one persistent launch that takes work from a queue,
+ * largest items first; FFBP merges run as one persistent launch per tree
+ * height across all scenes.  Each scene's output equals the single-scene entry
+ * point's (sarbp_backproject_lattice / sarbp_ffbp_execute, split mode) bit for
+ * bit when the tile shape is the same.  Inputs and outputs are bound at
+ * creation; execute never synchronises or allocates and is graph-capturable.
+ * No counterpart in the reference, which forms one scene at a time
+ * (BatchedResidentProgram, batched_resident_backend.py:23-157, batches the
+ * levels of one FFBP tree). */
+enum sarbp_batch_kind { SARBP_BATCH_DIRECT = 0, SARBP_BATCH_FFBP = 1 };
+
+typedef struct sarbp_batch_scene {
+    const float* data;            /* complex64 [pulses, samples] */
+    int pulses, samples;
+    const double* pos;            /* float64 [pulses, 3] */
+    const double* weight;         /* float64 [pulses] */
+    const double* phase;          /* float64 [pulses] */
+    double range_start, data_dr, k;
+    int kind;                     /* sarbp_batch_kind */
+    sarbp_lattice lattice;        /* DIRECT: the image lattice (step z components must be 0) */
+    const sarbp_ffbp_node* nodes; /* FFBP: plan nodes in pre-order (copied at creation) */
+    int n_nodes;
+    int crop_r0, crop_u0, crop_nr, crop_nu;
+    int tile_lc;                  /* DIRECT: log2 of tile columns, 2..5 (tile rows = 1024 >> tile_lc); 0 = 5 */
+    int chunk_pulses;             /* pulses staged per chunk (<= 32 used); 0 = default */
+    float* out;                   /* DIRECT: complex64 [rows, cols]; FFBP: complex64 [crop_nr, crop_nu] */
+} sarbp_batch_scene;
+
+typedef struct sarbp_batch sarbp_batch;
+
+/* blocks_per_sm: CTAs per SM of the persistent BP launch (0 = as many as fit). */
+int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks_per_sm, sarbp_batch** batch);
+void sarbp_batch_destroy(sarbp_batch* batch);
+size_t sarbp_batch_workspace_bytes(const sarbp_batch* batch);
+int sarbp_batch_launch_count(const sarbp_batch* batch);
+int sarbp_batch_info(const sarbp_batch* batch, int* bp_items, int* merge_items, int* max_height, int* bp_blocks,
+                     double* pixel_pulses);
+/* Uploads the scene, node and work tables into workspace (256-byte aligned); synchronises `stream`. */
+int sarbp_batch_bind(sarbp_batch* batch, void* workspace, size_t workspace_bytes, void* stream);
+int sarbp_batch_execute(const sarbp_batch* batch, void* stream);
+
 /* ---- autofocus helpers ---------------------------------------------------- */
 
 /* Zero-phase IIR filtering of each row of x (complex64 [rows, n]) with a

@@ -152,3 +152,42 @@ def test_scene_generation_is_seeded():
     assert a.lattice.points().shape == (32 * 32, 3)
     rmin, rmax, umin, umax = a.extent
     assert rmin < cfg.near_slant + 1 and rmax > rmin and umin < 0 < umax
+
+
+def test_batch_create_validates_scenes_on_host(lib):
+    h = lib.load()
+    fake = 0x10000  # never dereferenced: validation fails first
+    sc = (lib.BatchScene * 1)()
+    e = sc[0]
+    e.data = e.pos = e.weight = e.phase = e.out = fake
+    e.pulses, e.samples = 8, 64
+    e.range_start, e.data_dr, e.k = 90.0, 0.5, 1.0
+    e.kind = lib.BATCH_DIRECT
+    e.lattice = lib.lattice((0, 0, 0), (0.5, 0, 0.1), (0, 0.5, 0), 64, 64)  # tilted: not batchable
+    handle = ctypes.c_void_p()
+    assert h.sarbp_batch_create(sc, 1, 0, ctypes.byref(handle)) == lib.SARBP_ERR_VALUE
+    assert b"flat" in h.sarbp_last_error()
+    e.lattice = lib.lattice((0, 0, 0), (0.5, 0, 0), (0, 0.5, 0), 64, 64)
+    e.tile_lc = 7
+    assert h.sarbp_batch_create(sc, 1, 0, ctypes.byref(handle)) == lib.SARBP_ERR_VALUE
+    e.tile_lc = 0
+    e.kind = 5
+    assert h.sarbp_batch_create(sc, 1, 0, ctypes.byref(handle)) == lib.SARBP_ERR_VALUE
+    e.kind = lib.BATCH_FFBP  # FFBP scene without nodes
+    assert h.sarbp_batch_create(sc, 1, 0, ctypes.byref(handle)) == lib.SARBP_ERR_VALUE
+    e.data = 0
+    assert h.sarbp_batch_create(sc, 1, 0, ctypes.byref(handle)) == lib.SARBP_ERR_TYPE
+    assert h.sarbp_batch_create(sc, 0, 0, ctypes.byref(handle)) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_batch_execute(None, None) == lib.SARBP_ERR_TYPE
+
+
+def test_batch_scene_list_matches_the_uneven_workload():
+    from collections import Counter
+
+    from bp_project_gb300 import scenes
+    cfgs = scenes.batch_configs()
+    assert len(cfgs) == 64 and Counter(k for _, k in cfgs) == {"direct": 32, "ffbp": 32}
+    assert {c.pulses for c, _ in cfgs} <= set(range(512, 8193, 512))
+    assert {c.image_side for c, _ in cfgs} <= {256, 512, 1024, 2048}
+    assert all(3.5e3 <= c.near_slant <= 8e3 and 4 <= c.n_targets <= 16 for c, _ in cfgs)
+    assert scenes.batch_configs()[5][0] == cfgs[5][0]  # seeded
