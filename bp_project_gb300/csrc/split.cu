@@ -25,6 +25,7 @@
 // stored as zero, which reproduces the reference's support rule
 // (fast_bp/ffbp.py:27).  A tile whose window would not fit the staged bins
 // runs a chunk through an FP64 per-sample fallback instead.
+#include <limits.h>
 #include <math.h>
 
 #include "common.cuh"
@@ -64,6 +65,7 @@ struct TileShared {
     double scale_d, inv_scale_d;
     double sum[4];
     float bnd[3];               // bounds on |delta_x|, |delta_y|, |delta_z| (m)
+    float scale_f, inv_scale_f; // FP32 offset quantum of polar merge tiles
     float red[8][8];
     int base[kMaxChunk];        // global bin of window entry 0, per pulse of the chunk
     float wt[kMaxChunk];
@@ -281,8 +283,7 @@ __device__ __forceinline__ void quantize_pair(float& p, float& e, float q, float
     p = h;
 }
 
-__device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const float4* __restrict__ tables,
-                                Pix px[kPX]) {
+__device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const float4* __restrict__ tables) {
     const PolarDesc& g = J.g;
     const int tid = threadIdx.x;
     const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
@@ -334,19 +335,14 @@ __device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const floa
         const float mdc = fmaxf(fabsf(T.dcs[0]), fabsf(T.dcs[cl])), mdu = fmaxf(fabsf(T.duu[0]), fabsf(T.duu[cl]));
         const float bx = (mrx + mcx + mdg * mdc) * 1.0001f + 1e-6f;
         const float by = (mry + mcy + mdg * mdu) * 1.0001f + 1e-6f;
-        S.bnd[0] = bx;
-        S.bnd[1] = by;
-        S.bnd[2] = 0.0f;
-        S.rho = sqrt((double)bx * bx + (double)by * by);
-        set_quantum(S, fmaxf(bx, by), 12);
-        const double g0 = (double)r0v.x + (double)r0v.y;
-        const double c0 = (double)c0v.x + (double)c0v.y, u0 = (double)c0v.z + (double)c0v.w;
-        S.cx = g.ox + (double)g.side * g0 * c0;
-        S.cy = g.oy + g0 * u0;
-        S.cz = 0.0;
+        // Power-of-two quantum 2^(e - 12) with bound = m 2^e, m in [0.5, 1): FP32 bit arithmetic,
+        // no FP64 in this serial section (merges use only the quantum from the tile set-up).
+        const int e = ((__float_as_int(fmaxf(bx, by)) >> 23) & 0xff) - 126;
+        S.scale_f = __int_as_float((e - 12 + 127) << 23);
+        S.inv_scale_f = __int_as_float((12 - e + 127) << 23);
     }
     __syncthreads();
-    const float q = (float)S.scale_d, iq = (float)S.inv_scale_d;
+    const float q = S.scale_f, iq = S.inv_scale_f;
     if (tid < rows_t) {
         quantize_pair(T.rxh[tid], T.rxl[tid], q, iq);
         quantize_pair(T.ryh[tid], T.ryl[tid], q, iq);
@@ -356,23 +352,22 @@ __device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const floa
         quantize_pair(T.cyh[tid], T.cyl[tid], q, iq);
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kPX; ++k) {
-        const int p = tid + kThreads * k;
-        const int row = p >> J.lc, col = p & (cols_t - 1);
-        Pix& v = px[k];
-        v.dxh = T.rxh[row] + T.cxh[col];
-        v.dyh = T.ryh[row] + T.cyh[col];
-        v.dxl = fmaf(T.dg[row], T.dcs[col], T.rxl[row] + T.cxl[col]);
-        v.dyl = fmaf(T.dg[row], T.duu[col], T.ryl[row] + T.cyl[col]);
-        v.dzh = v.dzl = v.dz = 0.0f;
-        v.dx = v.dxh + v.dxl;
-        v.dy = v.dyh + v.dyl;
-        v.d2 = v.dx * v.dx + v.dy * v.dy;
-        v.psi = T.psi[row];
-        v.ar = v.ai = 0.0f;
-    }
-    __syncthreads();  // the tables alias the window region
+}
+
+// Offsets of tile pixel (row, col) from the tile centre, from the tables (FP32 pairs).
+__device__ __forceinline__ Pix tab_pixel(const TabF& T, int row, int col) {
+    Pix v;
+    v.dxh = T.rxh[row] + T.cxh[col];
+    v.dyh = T.ryh[row] + T.cyh[col];
+    v.dxl = fmaf(T.dg[row], T.dcs[col], T.rxl[row] + T.cxl[col]);
+    v.dyl = fmaf(T.dg[row], T.duu[col], T.ryl[row] + T.cyl[col]);
+    v.dzh = v.dzl = v.dz = 0.0f;
+    v.dx = v.dxh + v.dxl;
+    v.dy = v.dyh + v.dyl;
+    v.d2 = v.dx * v.dx + v.dy * v.dy;
+    v.psi = T.psi[row];
+    v.ar = v.ai = 0.0f;
+    return v;
 }
 
 template <bool HAS_Z>
@@ -1315,16 +1310,25 @@ __global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_s
     child_record(K, scale_w, inv_scale_w, nodes, items[t >> 1], t, arena, out);
 }
 
-__device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const Pix& q) {
+// Child-image coordinates of a parent pixel: bin indices (ir, iu), centred fractions
+// (sr, su) and the second-order range term eps.  ok: the 4x4 stencil lies inside the child.
+struct ChildCoord {
+    int ir, iu;
+    float sr, su, eps;
+    bool ok;
+};
+
+__device__ __forceinline__ ChildCoord child_coords(const ChildRec& R, const Pix& q) {
+    ChildCoord c;
     const float L = fmaf(R.b.x, q.dx, R.b.y * q.dy);
     const float q2 = fmaf(-L, L, q.d2);
     const float B = rcp_approx(fmaf(2.0f, L, R.b.z));
     const float e0 = q2 * B;
-    const float eps = fmaf(-e0 * e0, B, e0);
-    const float qr = fmaf(L + eps, R.inv_sdr, R.b.w);
+    c.eps = fmaf(-e0 * e0, B, e0);
+    const float qr = fmaf(L + c.eps, R.inv_sdr, R.b.w);
     const float tr = qr + kMagic;
-    const float sr = qr - (tr - kMagic);
-    const int ir = R.ir0 + (__float_as_int(tr) - kMagicBits);
+    c.sr = qr - (tr - kMagic);
+    c.ir = R.ir0 + (__float_as_int(tr) - kMagicBits);
     const float Lh = fmaf(R.c.y, q.dx, R.c.z * q.dy);
     const float q2h = fmaf(-Lh, Lh, q.d2);
     const float Bh = rcp_approx(fmaf(2.0f, Lh, R.c.w));
@@ -1334,14 +1338,20 @@ __device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const
     const float duu = fmaf(-R.c.z, dG, q.dy) * rcp_approx(gp);
     const float qu = fmaf(duu, R.inv_sdu, R.d.y);
     const float tu = qu + kMagic;
-    const float su = qu - (tu - kMagic);
-    const int iu = R.iu0 + (__float_as_int(tu) - kMagicBits);
+    c.su = qu - (tu - kMagic);
+    c.iu = R.iu0 + (__float_as_int(tu) - kMagicBits);
+    c.ok = c.ir >= 1 && c.ir <= R.snr - 3 && c.iu >= 1 && c.iu <= R.snu - 3 && gp > 0.0f;
+    return c;
+}
+
+__device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const Pix& q) {
+    const ChildCoord c = child_coords(R, q);
     float vr = 0.0f, vi = 0.0f;
-    if (ir >= 1 && ir <= R.snr - 3 && iu >= 1 && iu <= R.snu - 3 && gp > 0.0f) {
+    if (c.ok) {
         float wr[4], wu[4];
-        lagrange_centred(sr, wr);
-        lagrange_centred(su, wu);
-        const float2* base = R.img + (size_t)(ir - 1) * R.snu + (iu - 1);
+        lagrange_centred(c.sr, wr);
+        lagrange_centred(c.su, wu);
+        const float2* base = R.img + (size_t)(c.ir - 1) * R.snu + (c.iu - 1);
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const float2* row = base + (size_t)a * R.snu;
@@ -1358,7 +1368,7 @@ __device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const
         }
     }
     const float tb = fmaf(R.a.x, q.dxh, R.a.y * q.dyh);
-    float sm = fmaf(Kf, eps, R.c.x);
+    float sm = fmaf(Kf, c.eps, R.c.x);
     sm = fmaf(R.a.x, q.dxl, sm);
     sm = fmaf(R.a.y, q.dyl, sm);
     sm = fmaf(R.a.z, q.dx, sm);
@@ -1382,21 +1392,26 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
     if (threadIdx.x < 2) C[threadIdx.x] = crec[threadIdx.x];
-    Pix px[kPX];
     TabF& T = *reinterpret_cast<TabF*>(smem);
-    setup_polar_tab(J, S, T, tables, px);
-#pragma unroll
-    for (int k = 0; k < kPX; ++k) {
-        const float2 a = child_value(Kf, C[0], px[k]);
-        const float2 b = child_value(Kf, C[1], px[k]);
-        px[k].ar = __fadd_rn(a.x, b.x);
-        px[k].ai = __fadd_rn(a.y, b.y);
-    }
+    setup_polar_tab(J, S, T, tables);
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
-    store_window(J, J.g.win_nr, J.g.win_nu, px, dst, J.g.out_stride);
+    // One pixel at a time, its offsets read back from the shared tables: little state per
+    // thread keeps registers low and more warps resident to hide the child gathers' latency.
+    const int cols_t = 1 << J.lc;
+#pragma unroll 1
+    for (int k = 0; k < kPX; ++k) {
+        const int p = threadIdx.x + kThreads * k;
+        const int row = p >> J.lc, col = p & (cols_t - 1);
+        const Pix v = tab_pixel(T, row, col);
+        const float2 a = child_value(Kf, C[0], v);
+        const float2 b = child_value(Kf, C[1], v);
+        const int wr = J.tile_r + row, wu = J.tile_u + col;
+        if (wr < J.g.win_nr && wu < J.g.win_nu)
+            dst[(long long)wr * J.g.out_stride + wu] = make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+    }
 }
 
-__global__ void __launch_bounds__(kThreads, 3) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kThreads, 6) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
                                                                   const float4* __restrict__ tables,
                                                                   const ChildRec* __restrict__ crecs,
@@ -1429,6 +1444,8 @@ SplitParams make_params(const PulseInputs& in, int chunk, int cap, int pulse_spl
     P.envelope = kDirectEnvelope;
     return P;
 }
+
+size_t merge_smem() { return sizeof(TabF); }
 
 size_t dynamic_smem(int cap, bool polar) {
     size_t win = (size_t)cap * 32;
@@ -1627,7 +1644,7 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
     none.k = k;
     none.data_dr = 1.0;
     SplitParams P = make_params(none, 1, 4, 1);
-    const size_t smem = sizeof(TabF);
+    const size_t smem = merge_smem();
     if (int st = prepare(split_merge_kernel, smem)) return st;
     split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs),
                                                       arena, root_out, root);
@@ -1699,7 +1716,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_bp_kernel(const BatchScene*
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 3) batch_merge_kernel(const BatchScene* __restrict__ scenes,
+__global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchScene* __restrict__ scenes,
                                                                   const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items, int nitems,
                                                                   const float4* __restrict__ tables,
@@ -1761,11 +1778,11 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
 
 int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm) {
     if (int st = prepare(batch_bp_kernel, smem)) return st;
-    if (int st = prepare(batch_merge_kernel, sizeof(TabF))) return st;
+    if (int st = prepare(batch_merge_kernel, merge_smem())) return st;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bp_blocks_per_sm, batch_bp_kernel, kThreads, smem);
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_blocks_per_sm, batch_merge_kernel, kThreads,
-                                                          sizeof(TabF));
+                                                          merge_smem());
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
@@ -1809,7 +1826,8 @@ int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const 
                               const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
                               cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
-    batch_merge_kernel<<<blocks, kThreads, sizeof(TabF), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
+    if (int st = prepare(batch_merge_kernel, merge_smem())) return st;
+    batch_merge_kernel<<<blocks, kThreads, merge_smem(), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
                                                               items, nitems, tables,
                                                               reinterpret_cast<const ChildRec*>(crecs), arena,
                                                               counter);
