@@ -1398,7 +1398,7 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     // One pixel at a time, its offsets read back from the shared tables: little state per
     // thread keeps registers low and more warps resident to hide the child gathers' latency.
     const int cols_t = 1 << J.lc;
-#pragma unroll 1
+#pragma unroll 2
     for (int k = 0; k < kPX; ++k) {
         const int p = threadIdx.x + kThreads * k;
         const int row = p >> J.lc, col = p & (cols_t - 1);
