@@ -114,6 +114,7 @@ SIGNATURES = {
     "sarbp_ffbp_bind": ([_P, _P, _Z, _P], _I),
     "sarbp_ffbp_execute": ([_P, _P, _I, _I, _P, _P, _P, _D, _D, _D, _P, _P], _I),
     "sarbp_evaluate_image": ([_P, ctypes.POINTER(PolarGrid), _P, _I, _D, _P, _P], _I),
+    "sarbp_evaluate_lattice": ([_P, ctypes.POINTER(PolarGrid), ctypes.POINTER(Lattice), _D, _P, _P], _I),
     "sarbp_target_contributions": ([_P, _I, _I, _P, _P, _I, _D, _D, _D, _P, _P], _I),
     "sarbp_fill_range_phase_lut": ([_I, _D, _D, _D, _P, _P], _I),
     "sarbp_direct_polar_lut": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _P, _P, _P], _I),

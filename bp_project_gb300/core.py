@@ -175,6 +175,18 @@ def evaluate_image(image, grid: Grid, xyz, k, out=None):
     return out
 
 
+def evaluate_lattice(image, grid: Grid, origin, step_row, step_col, rows, cols, k, out=None):
+    """Polar image -> ground lattice origin + i*step_row + j*step_col (z ignored), split precision."""
+    _require(image, "image", torch.complex64, (grid.nr, grid.nu))
+    lat = nat.lattice(origin, step_row, step_col, rows, cols)
+    if out is None:
+        out = torch.empty((int(rows), int(cols)), dtype=torch.complex64, device=image.device)
+    _require(out, "out", torch.complex64, (int(rows), int(cols)))
+    nat.check(nat.load().sarbp_evaluate_lattice(_ptr(image), ctypes.byref(grid.native()), ctypes.byref(lat),
+                                                float(k), _ptr(out), stream_handle()), "evaluate_lattice")
+    return out
+
+
 def target_contributions(data, pos, xyz, range_start, data_dr, k, out=None):
     """Per target, per pulse sample1 * exp(jkr) (ffbp.target_contributions) -> complex64 [M, P]."""
     _require(data, "data", torch.complex64)

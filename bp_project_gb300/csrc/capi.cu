@@ -598,6 +598,20 @@ int sarbp_evaluate_image(const float* image, const sarbp_polar_grid* grid, const
                            reinterpret_cast<float2*>(out), (cudaStream_t)stream);
 }
 
+int sarbp_evaluate_lattice(const float* image, const sarbp_polar_grid* grid, const sarbp_lattice* lattice, double k,
+                           float* out, void* stream) {
+    if (!image || !lattice || !out) return fail(SARBP_ERR_TYPE, "image, lattice and out must not be NULL");
+    if (int st = check_grid(grid)) return st;
+    if (lattice->rows <= 0 || lattice->cols <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
+    for (int c = 0; c < 3; ++c)
+        if (!is_finite_value(lattice->origin[c]) || !is_finite_value(lattice->step_row[c]) ||
+            !is_finite_value(lattice->step_col[c]))
+            return fail(SARBP_ERR_VALUE, "lattice geometry must be finite");
+    if (!is_finite_value(k)) return fail(SARBP_ERR_VALUE, "k must be finite");
+    return launch_split_evaluate_lattice(reinterpret_cast<const float2*>(image), desc_of(*grid), *lattice, k,
+                                         reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
 int sarbp_target_contributions(const float* data, int pulses, int samples, const double* pos, const double* xyz,
                                int npts, double range_start, double data_dr, double k, float* out, void* stream) {
     if (!data || !pos || !xyz || !out) return fail(SARBP_ERR_TYPE, "data, pos, xyz and out must not be NULL");

@@ -193,6 +193,10 @@ int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const 
                               const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
                               cudaStream_t s);
 
+// Polar image -> flat ground lattice, split precision (evaluate_image on lattice points).
+int launch_split_evaluate_lattice(const float2* image, const PolarDesc& grid, const sarbp_lattice& lattice, double k,
+                                  float2* out, cudaStream_t s);
+
 // Zero-phase IIR smoothing along rows (autofocus phase-history filter).
 size_t sosfiltfilt_workspace(int rows, int n, int padlen);
 int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,

@@ -1262,19 +1262,11 @@ struct ChildRec {
 
 // One thread per (merge tile, child): the tile centre is the FP64 position of
 // the tile's centre pixel, the same point setup_polar_tab measures offsets from.
-__device__ __forceinline__ void child_record(double K, double scale_w, double inv_scale_w,
-                                             const PolarDesc* __restrict__ nodes, const TileItem it, int t,
-                                             float2* __restrict__ arena, ChildRec* __restrict__ out) {
-    const PolarDesc& g = nodes[it.node];
-    const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
-    const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
-    const int i0 = min(g.win_r0 + it.tile_r + (rows_t >> 1), g.nr - 1);
-    const int j0 = min(g.win_u0 + it.tile_u + (cols_t >> 1), g.nu - 1);
-    const double rc = g.r0 + (double)i0 * g.dr;
-    const double g0 = sqrt(fmax(0.0, rc * rc - g.oz * g.oz));
-    const double uc = g.u0 + (double)j0 * g.du;
-    const double c0 = sqrt(fmax(0.0, 1.0 - uc * uc));
-    const double vx = g.ox + (double)g.side * g0 * c0 - c.ox, vy = g.oy + g0 * uc - c.oy, vz = -c.oz;
+// FP64 record of a polar image c seen from the ground point (px, py, 0): the FP32
+// quantities child_value needs for points near it (a parent tile, or a lattice tile).
+__device__ __forceinline__ ChildRec child_rec_at(double K, double scale_w, double inv_scale_w, const PolarDesc& c,
+                                                 double px, double py, const float2* img) {
+    const double vx = px - c.ox, vy = py - c.oy, vz = -c.oz;
     const double g2 = vx * vx + vy * vy;
     const double G = sqrt(g2);
     const double RR = sqrt(g2 + vz * vz);
@@ -1298,8 +1290,24 @@ __device__ __forceinline__ void child_record(double K, double scale_w, double in
     R.iu0 = ok ? (int)iu : -(1 << 30);
     R.snr = c.nr;
     R.snu = c.nu;
-    R.img = arena + c.out_offset;
-    out[t] = R;
+    R.img = img;
+    return R;
+}
+
+__device__ __forceinline__ void child_record(double K, double scale_w, double inv_scale_w,
+                                             const PolarDesc* __restrict__ nodes, const TileItem it, int t,
+                                             float2* __restrict__ arena, ChildRec* __restrict__ out) {
+    const PolarDesc& g = nodes[it.node];
+    const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
+    const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
+    const int i0 = min(g.win_r0 + it.tile_r + (rows_t >> 1), g.nr - 1);
+    const int j0 = min(g.win_u0 + it.tile_u + (cols_t >> 1), g.nu - 1);
+    const double rc = g.r0 + (double)i0 * g.dr;
+    const double g0 = sqrt(fmax(0.0, rc * rc - g.oz * g.oz));
+    const double uc = g.u0 + (double)j0 * g.du;
+    const double c0 = sqrt(fmax(0.0, 1.0 - uc * uc));
+    out[t] = child_rec_at(K, scale_w, inv_scale_w, c, g.ox + (double)g.side * g0 * c0, g.oy + g0 * uc,
+                          arena + c.out_offset);
 }
 
 __global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_scale_w,
@@ -1652,6 +1660,38 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
     return check_launch("split_ffbp_merges");
 }
 
+// ---- polar image -> ground lattice (evaluate_image on a lattice, split precision) -----------
+//
+// A lattice tile is a parent tile whose pixels lie on the ground lattice, and the polar
+// image is its only child: one FP64 record per tile (child_rec_at at the tile centre),
+// then per pixel the merge kernel's FP32 child coordinates, 4x4 stencil and phase.  The
+// phase restores exp(j k r) (r: the point's range to the image origin); no demodulation.
+__global__ void __launch_bounds__(kThreads, 3) split_evaluate_lattice_kernel(double K, double scale_w,
+                                                                             double inv_scale_w, PolarDesc c,
+                                                                             const float2* __restrict__ img,
+                                                                             sarbp_lattice lat, int lc,
+                                                                             float2* __restrict__ out) {
+    __shared__ TileShared S;
+    __shared__ ChildRec C;
+    Job J;
+    J.lat = lat;
+    J.lc = lc;
+    tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
+    Pix px[kPX];
+    setup_lattice<false>(J, S, px);
+    if (threadIdx.x == 0) C = child_rec_at(K, scale_w, inv_scale_w, c, S.cx, S.cy, img);
+    __syncthreads();
+    const float Kf = (float)K;
+    const int cols_t = 1 << lc;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const float2 v = child_value(Kf, C, px[k]);
+        const int p = threadIdx.x + kThreads * k;
+        const int wr = J.tile_r + (p >> lc), wu = J.tile_u + (p & (cols_t - 1));
+        if (wr < lat.rows && wu < lat.cols) out[(long long)wr * lat.cols + wu] = v;
+    }
+}
+
 // ---- batched scenes: persistent work-queue kernels ------------------------------------------
 //
 // Many independent scenes (direct lattice images and FFBP trees) run as one work list.
@@ -1833,6 +1873,21 @@ int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const 
                                                               counter);
     note_launches(1);
     return check_launch("batch_merges");
+}
+
+int launch_split_evaluate_lattice(const float2* image, const PolarDesc& grid, const sarbp_lattice& lattice, double k,
+                                  float2* out, cudaStream_t s) {
+    PulseInputs none{};
+    none.k = k;
+    none.data_dr = 1.0;
+    const SplitParams P = make_params(none, 1, 4, 1);
+    sarbp_lattice flat = lattice;  // ground points: z is not used
+    flat.origin[2] = flat.step_row[2] = flat.step_col[2] = 0.0;
+    const int lc = 5;
+    split_evaluate_lattice_kernel<<<tiles_of(lattice.rows, lattice.cols, lc), kThreads, 0, s>>>(
+        P.K, P.scale_w, P.inv_scale_w, grid, image, flat, lc, out);
+    note_launches(1);
+    return check_launch("split_evaluate_lattice");
 }
 
 }  // namespace sarbp

@@ -289,6 +289,14 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
 int sarbp_evaluate_image(const float* image, const sarbp_polar_grid* grid, const double* xyz, int npts,
                          double k, float* out, void* stream);
 
+/* evaluate_image on the points of a ground lattice (z components ignored), out
+ * complex64 [rows, cols], in split precision: FP64 once per 32 x 32 pixel tile,
+ * FP32 per pixel (offsets as exact split products, phase reduced in turns).
+ * Same result as sarbp_evaluate_image on lattice points within ~1e-6 relative;
+ * run.py's ground image (run.py:120-125) is this call on its lattice. */
+int sarbp_evaluate_lattice(const float* image, const sarbp_polar_grid* grid, const sarbp_lattice* lattice, double k,
+                           float* out, void* stream);
+
 /* ffbp.target_contributions (ffbp.py:201-211): out[p, n] = sample1 * exp(j k r),
  * complex64 [npts, pulses]; FP64 geometry and phase. */
 int sarbp_target_contributions(const float* data, int pulses, int samples, const double* pos,

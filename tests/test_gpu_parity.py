@@ -98,6 +98,18 @@ def test_points_and_helpers(golden, lib):
     assert rel_err(g["evaluate"], ev) <= 1e-5
     tc = ffbp.target_contributions(g["data"], g["position"], g["targets"], r_start, ddr, k)
     assert rel_err(g["contrib"], tc) <= 1e-5
+    # The evaluation points are a lattice (x fastest): the split-precision lattice path matches too.
+    from bp_project_gb300 import core
+    pts = g["eval_points"]
+    xs, ys = np.unique(pts[:, 0]), np.unique(pts[:, 1])
+    assert len(xs) * len(ys) == len(pts)
+    image = torch.from_numpy(g["ffbp"]).cuda()
+    grid = core.Grid(tuple(ax[:3]), ax[3], ax[4], image.shape[0], ax[5], ax[6], image.shape[1], 1)
+    lat = core.evaluate_lattice(image, grid, (xs[0], ys[0], 0.0), (0.0, ys[1] - ys[0], 0.0), (xs[1] - xs[0], 0.0, 0.0),
+                                len(ys), len(xs), k)
+    err = rel_err(g["evaluate"], lat.cpu().numpy().ravel())
+    print(f"evaluate_lattice vs reference: {err:.3e}")
+    assert err <= 1e-5
     img, counts = ffbp.form_ffbp(g["data"], g["position"], r_start, ddr, fc, extent, leaf_size=32, range_spacing=0.5,
                                  angular_oversample=2.0, weight=g["weight"], verbose=False)
     assert img.image.shape == g["ffbp"].shape
@@ -152,6 +164,27 @@ def test_c0_full_image_vs_fp64_oracle(lib):
             np.unravel_index(amp[win].argmax(), amp[win].shape)
     mixed = _lattice_split(sc, mode="mixed").cpu().numpy()
     assert rel_err(full, mixed) <= 1e-5
+
+
+def test_evaluate_lattice_matches_points_path(lib):
+    """Split-precision evaluate onto the 512^2 ground lattice vs the FP64-geometry points kernel."""
+    from bp_project_gb300 import core
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    sc = _scene("c0")
+    cfg = sc.config
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    args = [_dev(a, dt) for a, dt in ((sc.data, torch.complex64), (sc.position, torch.float64),
+                                      (sc.weight, torch.float64), (sc.phase, torch.float64))]
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split", device="cuda")
+    polar = prog.execute(*args, sc.range_start, sc.data_dr, sc.k)
+    lat = sc.lattice
+    fast = core.evaluate_lattice(polar, plan.grid(), lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols, sc.k)
+    ref = core.evaluate_image(polar, plan.grid(), _dev(lat.points(), torch.float64), sc.k)
+    err = rel_err(ref.cpu().numpy(), fast.cpu().numpy().ravel())
+    print(f"evaluate_lattice vs points kernel: {err:.3e}")
+    assert err <= 1e-5
+    prog.close()
 
 
 @pytest.mark.slow
