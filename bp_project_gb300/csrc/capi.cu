@@ -294,6 +294,34 @@ int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples
                                         (cudaStream_t)stream);
 }
 
+int sarbp_rc_prepare(const float* raw, int pulses, int samples, int nfft, float* out, void* stream) {
+    if (!raw || !out) return fail(SARBP_ERR_TYPE, "raw and out must be device pointers");
+    if (pulses < 1 || samples < 1) return fail(SARBP_ERR_VALUE, "raw data must have at least one pulse and sample");
+    if (nfft < samples) return fail(SARBP_ERR_VALUE, "nfft (%d) must be >= samples (%d)", nfft, samples);
+    return launch_rc_prepare(reinterpret_cast<const float2*>(raw), pulses, samples, nfft, reinterpret_cast<float2*>(out),
+                             (cudaStream_t)stream);
+}
+
+int sarbp_rc_filter(const float* spectrum, const float* response, int pulses, int nfft, int length, float* out,
+                    void* stream) {
+    if (!spectrum || !response || !out) return fail(SARBP_ERR_TYPE, "spectrum, response and out must be device pointers");
+    if (pulses < 1 || nfft < 1) return fail(SARBP_ERR_VALUE, "pulses and nfft must be positive");
+    if (length < nfft) return fail(SARBP_ERR_VALUE, "length (%d) must be >= nfft (%d)", length, nfft);
+    if (length > nfft && (void*)spectrum == (void*)out) return fail(SARBP_ERR_VALUE, "oversampling cannot run in place");
+    return launch_rc_filter(reinterpret_cast<const float2*>(spectrum), reinterpret_cast<const float2*>(response),
+                            pulses, nfft, length, reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
+int sarbp_rc_crop(const float* corr, int pulses, int length, int offset, int samples, float scale, float* out,
+                  void* stream) {
+    if (!corr || !out) return fail(SARBP_ERR_TYPE, "corr and out must be device pointers");
+    if (pulses < 1 || samples < 1 || offset < 0 || offset + samples > length)
+        return fail(SARBP_ERR_VALUE, "crop window [%d, %d) outside the %d-sample correlation", offset, offset + samples,
+                    length);
+    return launch_rc_crop(reinterpret_cast<const float2*>(corr), pulses, length, offset, samples, scale,
+                          reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
 size_t sarbp_sosfiltfilt_workspace(int rows, int n, int padlen) {
     if (rows <= 0 || n <= 0 || padlen < 0) return 0;
     return sosfiltfilt_workspace(rows, n, padlen);

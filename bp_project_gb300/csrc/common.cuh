@@ -197,6 +197,13 @@ int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const 
 int launch_split_evaluate_lattice(const float2* image, const PolarDesc& grid, const sarbp_lattice& lattice, double k,
                                   float2* out, cudaStream_t s);
 
+// Range compression around the FFTs (mean removal + padding, filter + Fourier interpolation, crop).
+int launch_rc_prepare(const float2* raw, int pulses, int samples, int nfft, float2* out, cudaStream_t s);
+int launch_rc_filter(const float2* spec, const float2* response, int pulses, int nfft, int length, float2* out,
+                     cudaStream_t s);
+int launch_rc_crop(const float2* corr, int pulses, int length, int offset, int samples, float scale, float2* out,
+                   cudaStream_t s);
+
 // Zero-phase IIR smoothing along rows (autofocus phase-history filter).
 size_t sosfiltfilt_workspace(int rows, int n, int padlen);
 int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,

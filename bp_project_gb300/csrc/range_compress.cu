@@ -1,0 +1,132 @@
+// Range compression: the FFT matched filter that turns raw LFM echoes into the
+// range-compressed pulses the back-projection kernels consume (sar_io.range_compress,
+// fast_bp/sar_io.py:116-139).  The FFTs are library calls (cuFFT through the host);
+// these kernels are the memory-bound steps around them:
+//   rc_prepare  - remove each pulse's mean and zero-pad it to the FFT length,
+//   rc_filter   - multiply by the filter response and, when oversampling, place the
+//                 product in the longer spectrum (Fourier interpolation with the
+//                 Nyquist bin split in half, as scipy.signal.resample does),
+//   rc_crop     - cut the exact-lag window out of the correlation and scale it.
+// Each is one pass over its data: grid-stride loops, coalesced complex64 accesses.
+#include "common.cuh"
+
+namespace sarbp {
+namespace {
+
+constexpr int kRowThreads = 256;
+
+// One block per pulse: FP64 mean of the row, then the centred, zero-padded row.
+__global__ void rc_prepare_kernel(const float2* __restrict__ raw, int samples, int nfft, float2* __restrict__ out) {
+    const int row = blockIdx.x;
+    const float2* x = raw + (size_t)row * samples;
+    double sr = 0.0, si = 0.0;
+    for (int j = threadIdx.x; j < samples; j += kRowThreads) {
+        const float2 v = x[j];
+        sr += v.x;
+        si += v.y;
+    }
+    __shared__ double red[2][kRowThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][warp] = sr;
+        red[1][warp] = si;
+    }
+    __syncthreads();
+    double tr = 0.0, ti = 0.0;
+    for (int w = 0; w < kRowThreads / 32; ++w) {
+        tr += red[0][w];
+        ti += red[1][w];
+    }
+    const float mr = (float)(tr / samples), mi = (float)(ti / samples);  // complex64 mean, as the reference
+    float2* y = out + (size_t)row * nfft;
+    for (int j = threadIdx.x; j < nfft; j += kRowThreads) {
+        float2 v = make_float2(0.0f, 0.0f);
+        if (j < samples) {
+            const float2 a = x[j];
+            v = make_float2(a.x - mr, a.y - mi);
+        }
+        y[j] = v;
+    }
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// out[p, m] for m in [0, length): length == nfft multiplies in place order; a longer
+// length places bins [0, nfft/2] at the front and the negative frequencies at the back,
+// halving the positive Nyquist bin and copying it to the negative one (even nfft).
+__global__ void rc_filter_kernel(const float2* __restrict__ spec, const float2* __restrict__ response, int pulses,
+                                 int nfft, int length, float2* __restrict__ out) {
+    const long long total = (long long)pulses * length;
+    const int half = nfft / 2, nyq = nfft / 2 + 1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(t / length);
+        const int m = (int)(t - (long long)p * length);
+        const float2* s = spec + (size_t)p * nfft;
+        float2 v = make_float2(0.0f, 0.0f);
+        if (length == nfft) {
+            v = cmul(s[m], response[m]);
+        } else if (m < nyq) {
+            v = cmul(s[m], response[m]);
+            if ((nfft & 1) == 0 && m == half) v = make_float2(0.5f * v.x, 0.5f * v.y);
+        } else if (m >= length - (nfft - nyq)) {
+            const int k = m - length + nfft;  // negative frequency bin of the short spectrum
+            v = cmul(s[k], response[k]);
+        } else if ((nfft & 1) == 0 && m == length - half) {
+            v = cmul(s[half], response[half]);
+            v = make_float2(0.5f * v.x, 0.5f * v.y);
+        }
+        out[t] = v;
+    }
+}
+
+__global__ void rc_crop_kernel(const float2* __restrict__ corr, int pulses, int length, int offset, int samples,
+                               float scale, float2* __restrict__ out) {
+    const long long total = (long long)pulses * samples;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int p = (int)(t / samples);
+        const int j = (int)(t - (long long)p * samples);
+        const float2 v = corr[(size_t)p * length + offset + j];
+        out[t] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+int stream_grid(long long n) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long blocks = (n + kRowThreads - 1) / kRowThreads;
+    return (int)(blocks < 8LL * sms ? (blocks > 0 ? blocks : 1) : 8LL * sms);
+}
+
+}  // namespace
+
+int launch_rc_prepare(const float2* raw, int pulses, int samples, int nfft, float2* out, cudaStream_t s) {
+    rc_prepare_kernel<<<pulses, kRowThreads, 0, s>>>(raw, samples, nfft, out);
+    note_launches(1);
+    return check_launch("rc_prepare");
+}
+
+int launch_rc_filter(const float2* spec, const float2* response, int pulses, int nfft, int length, float2* out,
+                     cudaStream_t s) {
+    rc_filter_kernel<<<stream_grid((long long)pulses * length), kRowThreads, 0, s>>>(spec, response, pulses, nfft,
+                                                                                    length, out);
+    note_launches(1);
+    return check_launch("rc_filter");
+}
+
+int launch_rc_crop(const float2* corr, int pulses, int length, int offset, int samples, float scale, float2* out,
+                   cudaStream_t s) {
+    rc_crop_kernel<<<stream_grid((long long)pulses * samples), kRowThreads, 0, s>>>(corr, pulses, length, offset,
+                                                                                   samples, scale, out);
+    note_launches(1);
+    return check_launch("rc_crop");
+}
+
+}  // namespace sarbp

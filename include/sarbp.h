@@ -228,6 +228,25 @@ int sarbp_batch_info(const sarbp_batch* batch, int* bp_items, int* merge_items, 
 int sarbp_batch_bind(sarbp_batch* batch, void* workspace, size_t workspace_bytes, void* stream);
 int sarbp_batch_execute(const sarbp_batch* batch, void* stream);
 
+/* ---- range compression (sar_io.range_compress, sar_io.py:116-139) --------- */
+
+/* The matched filter that produces BP's input: y = crop(ifft(fft(pad(x - mean x))
+ * * fft(h))) with h the conjugated, reversed, Hamming-weighted LFM reference.
+ * The FFTs are library calls made by the host between these steps:
+ *   sarbp_rc_prepare: out [pulses, nfft] = each pulse minus its mean, zero-padded;
+ *   sarbp_rc_filter:  out [pulses, length] = spectrum * response (both [.., nfft]),
+ *                     placed in a length = nfft * oversample spectrum for Fourier
+ *                     interpolation with the even-length Nyquist bin split in half
+ *                     (scipy.signal.resample); length == nfft multiplies in place
+ *                     if out == spectrum;
+ *   sarbp_rc_crop:    out [pulses, samples] = scale * corr[:, offset : offset + samples].
+ * All arrays are complex64. */
+int sarbp_rc_prepare(const float* raw, int pulses, int samples, int nfft, float* out, void* stream);
+int sarbp_rc_filter(const float* spectrum, const float* response, int pulses, int nfft, int length, float* out,
+                    void* stream);
+int sarbp_rc_crop(const float* corr, int pulses, int length, int offset, int samples, float scale, float* out,
+                  void* stream);
+
 /* ---- autofocus helpers ---------------------------------------------------- */
 
 /* Zero-phase IIR filtering of each row of x (complex64 [rows, n]) with a

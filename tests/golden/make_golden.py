@@ -39,6 +39,10 @@ autofocus.npz
     polar image.  matplotlib is absent here, so an empty module stands in
     for it (autofocus.py only plots in ``main``).
 
+range_compress.npz
+    ``sar_io.range_compress`` (fast_bp/sar_io.py:116-139) on seeded raw
+    echoes (oversample 1 and 2), and the lag of the LFM point test of
+    ``validate.py:54-59`` (oversample 4).
 metrics.npz
     ``sar_quality/metrics.py`` (focus_metrics, fidelity, impulse_metrics) on
     seeded images and impulse cuts.  numpy 2 removed ``trapz``; the
@@ -283,6 +287,36 @@ def autofocus_case():
     return out
 
 
+def range_compress_inputs():
+    """Seeded raw echoes for the range-compression golden case (rebuilt by the tests)."""
+    rng = np.random.default_rng(1160)
+    raw = (rng.standard_normal((6, 700)) + 1j * rng.standard_normal((6, 700))).astype(np.complex64)
+    fs = 400e6
+    t = (np.arange(700) - 311.7) / fs  # one chirp centred at a fractional sample, plus noise
+    raw[2] += (3 * np.exp(-1j * np.pi * 200e6 / 1e-6 * t ** 2) * (np.abs(t) < 0.5e-6)).astype(np.complex64)
+    return raw
+
+
+def lfm_point_raw():
+    """validate.py:55-56: one LFM echo centred at sample 1512.4 of 4000."""
+    fs = 400e6
+    tr = (np.arange(4000) - 1512.4) / fs
+    return (np.exp(-1j * np.pi * 200e6 / 1e-6 * tr ** 2) * (np.abs(tr) < 0.5e-6)).astype(np.complex64)[None, :]
+
+
+def range_compress_case(root):
+    sys.path.insert(0, str(root / "fast_bp"))
+    import sar_io  # noqa: E402
+    raw = range_compress_inputs()
+    out = {"os1": sar_io.range_compress(raw), "os2": sar_io.range_compress(raw, oversample=2),
+           "os1_up": sar_io.range_compress(raw, chirp_sign=1, tp=0.8e-6, bandwidth=150e6)}
+    lfm = sar_io.range_compress(lfm_point_raw(), oversample=4)
+    out["lfm_peak"] = np.array(np.argmax(np.abs(lfm[0])) / 4)
+    out["lfm_near_peak"] = lfm[0, 6000:6100]
+    print(f"range_compress: lfm peak {float(out['lfm_peak']):.3f} (echo at 1512.4)", flush=True)
+    return out
+
+
 def metrics_cases():
     """Seeded inputs of the metrics golden case (rebuilt by the tests)."""
     rng = np.random.default_rng(515)
@@ -329,6 +363,7 @@ CASES = {
     "plans": lambda ffbp, gb: plans_case(gb),
     "autofocus": lambda ffbp, gb: autofocus_case(),
     "metrics": lambda ffbp, gb: metrics_case(ROOT_ARG[0]),
+    "range_compress": lambda ffbp, gb: range_compress_case(ROOT_ARG[0]),
 }
 ROOT_ARG = [Path("/root/reference")]
 

@@ -191,3 +191,12 @@ def test_batch_scene_list_matches_the_uneven_workload():
     assert {c.image_side for c, _ in cfgs} <= {256, 512, 1024, 2048}
     assert all(3.5e3 <= c.near_slant <= 8e3 and 4 <= c.n_targets <= 16 for c, _ in cfgs)
     assert scenes.batch_configs()[5][0] == cfgs[5][0]  # seeded
+
+
+def test_range_compress_entry_points_validate_on_host(lib):
+    h = lib.load()
+    fake = ctypes.c_void_p(0x10000)
+    assert h.sarbp_rc_prepare(None, 4, 100, 128, fake, None) == lib.SARBP_ERR_TYPE
+    assert h.sarbp_rc_prepare(fake, 4, 100, 50, fake, None) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_rc_filter(fake, fake, 4, 128, 100, fake, None) == lib.SARBP_ERR_VALUE
+    assert h.sarbp_rc_crop(fake, 4, 100, 60, 50, 1.0, fake, None) == lib.SARBP_ERR_VALUE
