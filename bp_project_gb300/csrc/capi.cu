@@ -322,6 +322,19 @@ int sarbp_rc_crop(const float* corr, int pulses, int length, int offset, int sam
                           reinterpret_cast<float2*>(out), (cudaStream_t)stream);
 }
 
+int sarbp_decode_iq(const void* frames, int n, long long frame_size, int iq_offset, int nr, float* out,
+                    void* stream) {
+    if (!frames || !out) return fail(SARBP_ERR_TYPE, "frames and out must be device pointers");
+    if (n < 1 || nr < 1) return fail(SARBP_ERR_VALUE, "at least one frame and one sample are required");
+    if (iq_offset < 0 || (long long)iq_offset + 4LL * nr > frame_size)
+        return fail(SARBP_ERR_VALUE, "I/Q block [%d, %lld) outside the %lld-byte frame", iq_offset,
+                    (long long)iq_offset + 4LL * nr, frame_size);
+    if (((uintptr_t)frames & 3) || (frame_size & 3) || (iq_offset & 3))
+        return fail(SARBP_ERR_TYPE, "frames, frame_size and iq_offset must be 4-byte aligned");
+    return launch_decode_iq(reinterpret_cast<const unsigned char*>(frames), n, frame_size, iq_offset, nr,
+                            reinterpret_cast<float2*>(out), (cudaStream_t)stream);
+}
+
 size_t sarbp_sosfiltfilt_workspace(int rows, int n, int padlen) {
     if (rows <= 0 || n <= 0 || padlen < 0) return 0;
     return sosfiltfilt_workspace(rows, n, padlen);

@@ -203,6 +203,8 @@ int launch_rc_filter(const float2* spec, const float2* response, int pulses, int
                      cudaStream_t s);
 int launch_rc_crop(const float2* corr, int pulses, int length, int offset, int samples, float scale, float2* out,
                    cudaStream_t s);
+int launch_decode_iq(const unsigned char* frames, int n, long long frame_size, int iq_offset, int nr, float2* out,
+                     cudaStream_t s);
 
 // Zero-phase IIR smoothing along rows (autofocus phase-history filter).
 size_t sosfiltfilt_workspace(int rows, int n, int padlen);

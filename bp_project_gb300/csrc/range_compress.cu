@@ -8,6 +8,7 @@
 //                 Nyquist bin split in half, as scipy.signal.resample does),
 //   rc_crop     - cut the exact-lag window out of the correlation and scale it.
 // Each is one pass over its data: grid-stride loops, coalesced complex64 accesses.
+// decode_iq turns raw capture frames (int16 I/Q after a header) into complex64 pulses.
 #include "common.cuh"
 
 namespace sarbp {
@@ -60,8 +61,9 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 // out[p, m] for m in [0, length): length == nfft multiplies in place order; a longer
 // length places bins [0, nfft/2] at the front and the negative frequencies at the back,
 // halving the positive Nyquist bin and copying it to the negative one (even nfft).
-__global__ void rc_filter_kernel(const float2* __restrict__ spec, const float2* __restrict__ response, int pulses,
-                                 int nfft, int length, float2* __restrict__ out) {
+// spec and out may be the same array (length == nfft): no __restrict__ on either.
+__global__ void rc_filter_kernel(const float2* spec, const float2* __restrict__ response, int pulses, int nfft,
+                                 int length, float2* out) {
     const long long total = (long long)pulses * length;
     const int half = nfft / 2, nyq = nfft / 2 + 1;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -98,6 +100,18 @@ __global__ void rc_crop_kernel(const float2* __restrict__ corr, int pulses, int 
     }
 }
 
+// Raw frames -> complex64: frame i's I/Q pairs start iq_offset bytes into the frame.
+__global__ void decode_iq_kernel(const unsigned char* __restrict__ frames, int n, long long frame_size, int iq_offset,
+                                 int nr, float2* __restrict__ out) {
+    const long long total = (long long)n * nr;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long i = t / nr, j = t - i * nr;
+        const short2 v = *reinterpret_cast<const short2*>(frames + i * frame_size + iq_offset + 4 * j);
+        out[t] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
 int stream_grid(long long n) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -119,6 +133,13 @@ int launch_rc_filter(const float2* spec, const float2* response, int pulses, int
                                                                                     length, out);
     note_launches(1);
     return check_launch("rc_filter");
+}
+
+int launch_decode_iq(const unsigned char* frames, int n, long long frame_size, int iq_offset, int nr, float2* out,
+                     cudaStream_t s) {
+    decode_iq_kernel<<<stream_grid((long long)n * nr), kRowThreads, 0, s>>>(frames, n, frame_size, iq_offset, nr, out);
+    note_launches(1);
+    return check_launch("decode_iq");
 }
 
 int launch_rc_crop(const float2* corr, int pulses, int length, int offset, int samples, float scale, float2* out,

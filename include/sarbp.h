@@ -247,6 +247,13 @@ int sarbp_rc_filter(const float* spectrum, const float* response, int pulses, in
 int sarbp_rc_crop(const float* corr, int pulses, int length, int offset, int samples, float scale, float* out,
                   void* stream);
 
+/* Raw capture frames -> complex64 pulses (sar_io.Capture.read, sar_io.py:79-81):
+ * out [n, nr] = I + jQ from the little-endian int16 pairs that start iq_offset bytes
+ * into each of n consecutive frames of frame_size bytes (device memory).  frames,
+ * frame_size and iq_offset must be 4-byte aligned (the capture format's are). */
+int sarbp_decode_iq(const void* frames, int n, long long frame_size, int iq_offset, int nr, float* out,
+                    void* stream);
+
 /* ---- autofocus helpers ---------------------------------------------------- */
 
 /* Zero-phase IIR filtering of each row of x (complex64 [rows, n]) with a

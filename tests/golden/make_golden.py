@@ -43,6 +43,10 @@ range_compress.npz
     ``sar_io.range_compress`` (fast_bp/sar_io.py:116-139) on seeded raw
     echoes (oversample 1 and 2), and the lag of the LFM point test of
     ``validate.py:54-59`` (oversample 4).
+capture.npz
+    ``sar_io.Capture`` (fast_bp/sar_io.py:18-82) on the synthetic raw capture
+    written by ``capture_file.py``: frame count, valid frames, timing fields,
+    navigation and ``read`` of a few pulses.
 metrics.npz
     ``sar_quality/metrics.py`` (focus_metrics, fidelity, impulse_metrics) on
     seeded images and impulse cuts.  numpy 2 removed ``trapz``; the
@@ -317,6 +321,28 @@ def range_compress_case(root):
     return out
 
 
+def capture_case(root):
+    import tempfile
+    sys.path.insert(0, str(root / "fast_bp"))
+    sys.path.insert(0, str(HERE))
+    import sar_io  # noqa: E402
+    from capture_file import write_capture
+    with tempfile.TemporaryDirectory() as tmp:
+        cap = sar_io.Capture(write_capture(Path(tmp) / "capture.dat"))
+        idx = np.array([0, 3, 4, 10, cap.n - 1])
+        out = {"n": np.array(cap.n), "nr": np.array(cap.nr), "offset": np.array(cap.offset),
+               "frame_size": np.array(cap.frame_size), "valid_indices": cap.valid_indices,
+               "scalars": np.array([cap.tp, cap.delay, cap.prf, cap.bandwidth]), "time": cap.time,
+               "read_idx": idx, "read": cap.read(idx)}
+        for k, v in cap.nav.items():
+            out["nav_" + k] = v
+        out["summary"] = np.array([cap.summary[k] for k in ("complete_frame_slots", "valid_frames", "invalid_slots",
+                                                             "first_pulse", "last_pulse", "missing_pulses",
+                                                             "discarded_partial_bytes")])
+    print(f"capture: {cap.n} valid frames of {cap.nr} samples", flush=True)
+    return out
+
+
 def metrics_cases():
     """Seeded inputs of the metrics golden case (rebuilt by the tests)."""
     rng = np.random.default_rng(515)
@@ -364,6 +390,7 @@ CASES = {
     "autofocus": lambda ffbp, gb: autofocus_case(),
     "metrics": lambda ffbp, gb: metrics_case(ROOT_ARG[0]),
     "range_compress": lambda ffbp, gb: range_compress_case(ROOT_ARG[0]),
+    "capture": lambda ffbp, gb: capture_case(ROOT_ARG[0]),
 }
 ROOT_ARG = [Path("/root/reference")]
 

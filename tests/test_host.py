@@ -200,3 +200,11 @@ def test_range_compress_entry_points_validate_on_host(lib):
     assert h.sarbp_rc_prepare(fake, 4, 100, 50, fake, None) == lib.SARBP_ERR_VALUE
     assert h.sarbp_rc_filter(fake, fake, 4, 128, 100, fake, None) == lib.SARBP_ERR_VALUE
     assert h.sarbp_rc_crop(fake, 4, 100, 60, 50, 1.0, fake, None) == lib.SARBP_ERR_VALUE
+
+
+def test_decode_iq_validates_on_host(lib):
+    h = lib.load()
+    fake = ctypes.c_void_p(0x10000)
+    assert h.sarbp_decode_iq(None, 4, 1152, 160, 240, fake, None) == lib.SARBP_ERR_TYPE
+    assert h.sarbp_decode_iq(fake, 4, 1152, 160, 300, fake, None) == lib.SARBP_ERR_VALUE  # I/Q past the frame
+    assert h.sarbp_decode_iq(fake, 4, 1150, 160, 240, fake, None) == lib.SARBP_ERR_TYPE   # misaligned frames
