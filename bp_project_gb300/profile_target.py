@@ -7,8 +7,11 @@ its kernels:
     python -m bp_project_gb300.profile_target --workload ffbp   --config c1 --reps 2
 
 Workloads: ``direct`` (split-precision direct BP on the scene's ground
-lattice), ``ffbp`` (level-batched FFBP + evaluate_image onto the lattice),
-``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice).
+lattice), ``ffbp`` (level-batched FFBP + split evaluation onto the lattice),
+``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice),
+``adjoint`` (forward + adjoint of lattice BP, the entropy autofocus step),
+``range`` (range compression of the scene's data treated as raw echoes),
+``batch`` (a small uneven scene batch through the persistent kernels).
 Prints one JSON line with event timings (not for benchmarking under a
 profiler: bench.py is the benchmark).
 """
@@ -25,7 +28,7 @@ from .gpu_backend import build_ffbp_plan
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=("direct", "ffbp", "plain"), default="direct")
+    ap.add_argument("--workload", choices=("direct", "ffbp", "plain", "adjoint", "range", "batch"), default="direct")
     ap.add_argument("--config", default="c1")
     ap.add_argument("--pulses", type=int, default=None, help="scale the scene to this many pulses")
     ap.add_argument("--side", type=int, default=None, help="scale the ground image to side x side pixels")
@@ -55,17 +58,55 @@ def main(argv=None):
             core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, rows, lat.cols,
                                      scene.range_start, scene.data_dr, scene.k, mode=mode, out=out)
         units = rows * lat.cols * cfg.pulses
+    elif args.workload == "adjoint":
+        from .autofocus import image_entropy
+        from .autograd import backproject_lattice
+        geo = (tuple(lat.origin), tuple(lat.step_row), tuple(lat.step_col), lat.rows, lat.cols, scene.range_start,
+               scene.data_dr, scene.k)
+
+        def run():
+            p = pos.clone().requires_grad_()
+            f = ph.clone().requires_grad_()
+            image_entropy(backproject_lattice(data, p, wt, f, *geo)).backward()
+        units = lat.rows * lat.cols * cfg.pulses
+    elif args.workload == "range":
+        from .sar_io import range_compress
+
+        def run():
+            range_compress(data, tp=1e-6, bandwidth=cfg.bandwidth, oversample=1, fs=cfg.fs)
+        units = data.numel()
+    elif args.workload == "batch":
+        from .batch import DirectScene, FFBPScene, SceneBatch
+        items = []
+        for c, kind in scenes.batch_configs(count=8, seed=11, pulse_choices=(1024, 2048), side_choices=(512, 1024)):
+            sc = scenes.synthesize(c, device="cuda")
+            common = dict(data=torch.from_numpy(sc.data).to(dev), pos=torch.from_numpy(sc.position).to(dev),
+                          weight=torch.from_numpy(sc.weight).to(dev), phase=torch.from_numpy(sc.phase).to(dev),
+                          range_start=sc.range_start, data_dr=sc.data_dr, k=sc.k)
+            if kind == "direct":
+                L = sc.lattice
+                items.append(DirectScene(**common, origin=tuple(L.origin), step_row=tuple(L.step_row),
+                                         step_col=tuple(L.step_col), rows=L.rows, cols=L.cols))
+            else:
+                pl = build_ffbp_plan(sc.position, c.fc, sc.extent, side=1, leaf_size=c.leaf_size,
+                                     range_spacing=c.range_spacing, angular_oversample=c.angular_oversample)
+                items.append(FFBPScene(**common, plan=pl))
+        batch = SceneBatch(items)
+
+        def run():
+            batch.execute()
+        units = batch.info["pixel_pulses"]
     else:
         plan = build_ffbp_plan(scene.position, cfg.fc, scene.extent, side=1, leaf_size=cfg.leaf_size,
                                range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
         prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode=args.mode, device=dev)
-        pts = torch.from_numpy(lat.points()).to(dev)
-        ground = torch.empty(lat.rows * lat.cols, dtype=torch.complex64, device=dev)
+        ground = torch.empty((lat.rows, lat.cols), dtype=torch.complex64, device=dev)
         grid = plan.grid()
 
         def run():
             polar = prog.execute(data, pos, wt, ph, scene.range_start, scene.data_dr, scene.k)
-            core.evaluate_image(polar, grid, pts, scene.k, out=ground)
+            core.evaluate_lattice(polar, grid, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols, scene.k,
+                                  out=ground)
         units = lat.rows * lat.cols * cfg.pulses
     for _ in range(args.reps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
