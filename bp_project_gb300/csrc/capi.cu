@@ -600,7 +600,7 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
         double span = 0.0;
         for (int i : plan->leaves) span = std::max(span, 32.0 * fabs(plan->nodes[i].dr));
         const int wb = (int)ceil(span / fabs(data_dr)) + 48;
-        const int ch = split_chunk_for(wb, plan->leaf_chunk);
+        const int ch = split_chunk_for(wb, plan->leaf_chunk, true);
         st = launch_split_ffbp_tables(in, nodes, plan->n_nodes, plan->max_dim, tables, s);
         if (st == SARBP_OK)
             st = launch_split_ffbp_leaf_pulses(in, nodes, leaves, (int)plan->leaves.size(), precs, s);

@@ -16,16 +16,26 @@ namespace {
 
 constexpr int kRowThreads = 256;
 
-// One block per pulse: FP64 mean of the row, then the centred, zero-padded row.
+// One block per pulse: the row's mean (FP32 partial sums per thread, FP64 across threads),
+// then the centred, zero-padded row.  Rows are read as float4 pairs when 16-byte aligned.
 __global__ void rc_prepare_kernel(const float2* __restrict__ raw, int samples, int nfft, float2* __restrict__ out) {
     const int row = blockIdx.x;
     const float2* x = raw + (size_t)row * samples;
-    double sr = 0.0, si = 0.0;
-    for (int j = threadIdx.x; j < samples; j += kRowThreads) {
-        const float2 v = x[j];
-        sr += v.x;
-        si += v.y;
+    float pr = 0.0f, pi = 0.0f;
+    const bool vec = ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+    const int pairs = vec ? samples / 2 : 0;
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    for (int j = threadIdx.x; j < pairs; j += kRowThreads) {
+        const float4 v = x4[j];
+        pr += v.x + v.z;
+        pi += v.y + v.w;
     }
+    for (int j = 2 * pairs + threadIdx.x; j < samples; j += kRowThreads) {
+        const float2 v = x[j];
+        pr += v.x;
+        pi += v.y;
+    }
+    double sr = pr, si = pi;
     __shared__ double red[2][kRowThreads / 32];
     for (int o = 16; o > 0; o >>= 1) {
         sr += __shfl_xor_sync(0xffffffffu, sr, o);

@@ -37,8 +37,10 @@ constexpr int kThreads = kSplitThreads;
 constexpr int kPX = 4;
 constexpr int kMaxRows = kSplitTilePixels >> 2;  // tile_lc >= 2
 constexpr int kMaxCols = 32;                     // tile_lc <= 5
-constexpr int kMaxChunk = 32;                    // one warp computes a chunk's records
-constexpr int kWindowBudget = 96 * 1024;
+constexpr int kMaxChunk = 64;      // pulses per chunk of the direct kernels: two warps compute the records
+constexpr int kMaxLeafChunk = 32;  // pulses per chunk of the FFBP leaf kernels: one warp computes the records
+// Window bytes per CTA: with kMaxChunk records this keeps three CTAs per SM within 227 KB.
+constexpr int kWindowBudget = 68 * 1024;
 // K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
 // error, FFBP leaves 1e-4.
 constexpr double kDirectEnvelope = 8.0;
@@ -70,6 +72,8 @@ struct TileShared {
     int base[kMaxChunk];        // global bin of window entry 0, per pulse of the chunk
     float wt[kMaxChunk];
     int nfit;
+    int nfit_w[2];              // fitting pulses among each record warp's 32
+    int wsum;                   // window entries of record warp 0's pulses
 };
 
 // Row/column tables of a polar tile; aliased onto the window region during set-up.
@@ -492,8 +496,11 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
                 sm = fmaf(rd.z, q.dz, sm);
             }
             if (DEMOD) sm += q.psi;
-            const float tot = (tb - round_magic(tb)) + sm;
-            const float ang = (tot - round_magic(tot)) * kTwoPiF;
+            // The reduced large term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps <= 1 + envelope / 2
+            // turns (5 turns for direct tiles), so the angle stays within +-40 rad: the hardware
+            // sin/cos reduce it themselves with an absolute error below 3e-6 rad, and a second
+            // reduction in turns is not needed.
+            const float ang = ((tb - round_magic(tb)) + sm) * kTwoPiF;
             float sn, cs;
             __sincosf(ang, &sn, &cs);
             q.ar = fmaf(vr, cs, q.ar);
@@ -579,11 +586,12 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
     return count;
 }
 
-// Chunk driver shared by the forward and adjoint kernels: per chunk, warp 0
-// computes the (tile, pulse) records and packs the pulses' range windows, all
-// warps stage the windows (Horner coefficients, times the pulse weight when
-// `weighted`), then `body.fast(rec, win, nfit, c0)` consumes them; a pulse
-// whose window cannot be staged goes through `body.slow(c0)`.
+// Chunk driver shared by the forward and adjoint kernels: per chunk of up to 64
+// pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, FP64,
+// on two SM sub-partitions at once) and pack the pulses' range windows, all warps
+// stage the windows (Horner coefficients, times the pulse weight when `weighted`),
+// then `body.fast(rec, win, nfit, c0)` consumes them; a pulse whose window cannot be
+// staged goes through `body.slow(c0)`.
 template <class Body>
 __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, bool weighted, Body& body) {
     const PulseInputs& in = P.in;
@@ -593,21 +601,25 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
     for (int c0 = J.p0; c0 < J.p1;) {
         const int want = min(P.chunk, J.p1 - c0);
         __syncthreads();  // the previous chunk's records and windows are consumed
-        if (warp == 0) {
-            const int count = lane < want ? make_record(P, S, rec, lane, c0 + lane) : 0;
+        if (warp < 2) {
+            const int idx = 32 * warp + lane;
+            const int count = idx < want ? make_record(P, S, rec, idx, c0 + idx) : 0;
             int inc = count;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int v = __shfl_up_sync(0xffffffffu, inc, o);
                 if (lane >= o) inc += v;
             }
+            if (warp == 0 && lane == 31) S.wsum = inc;
+            asm volatile("bar.sync 2, 64;" ::: "memory");  // warps 0 and 1 only
+            if (warp == 1) inc += S.wsum;
             // Counts are >= 1, so the pulses that fit form a prefix of the chunk.
-            const unsigned fits = __ballot_sync(0xffffffffu, lane < want && inc <= P.cap);
-            if (lane < want) rec[lane].c.z = __int_as_float(inc - count);
-            if (lane == 0) S.nfit = __popc(fits);
+            const unsigned fits = __ballot_sync(0xffffffffu, idx < want && inc <= P.cap);
+            if (idx < want) rec[idx].c.z = __int_as_float(inc - count);
+            if (lane == 0) S.nfit_w[warp] = __popc(fits);
         }
         __syncthreads();
-        const int nfit = S.nfit;
+        const int nfit = S.nfit_w[0] + S.nfit_w[1];
         if (nfit > 0) {
             for (int nl = warp; nl < nfit; nl += kThreads / 32) {
                 const int off = __float_as_int(rec[nl].c.z);
@@ -945,17 +957,35 @@ __global__ void __launch_bounds__(kThreads, 2) split_lattice_adjoint_kernel(Spli
     chunk_loop(P, J, S, smem, false, body);
 }
 
-// Per-pulse gradients from the tiles' partial sums, added in tile order (deterministic).
-__global__ void adjoint_sum_kernel(const float* __restrict__ partials, int ntiles, int pulses,
-                                   const double* __restrict__ weight, double* grad_pos, double* grad_phase,
-                                   double* grad_weight) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= pulses) return;
+// Per-pulse gradients from the tiles' partial sums, in a fixed order (deterministic): each
+// block takes 32 pulses; its 8 thread groups sum every 8th tile (coalesced: for one tile the
+// 32 pulses' values are contiguous), then the 8 group sums are added in group order.
+constexpr int kSumPulses = 32, kSumGroups = kThreads / kSumPulses;
+
+__global__ void __launch_bounds__(kThreads) adjoint_sum_kernel(const float* __restrict__ partials, int ntiles,
+                                                               int pulses, const double* __restrict__ weight,
+                                                               double* grad_pos, double* grad_phase,
+                                                               double* grad_weight) {
+    __shared__ double part[kSumGroups][kSumPulses][kAdjVals];
+    const int pl = threadIdx.x % kSumPulses, grp = threadIdx.x / kSumPulses;
+    const int n = blockIdx.x * kSumPulses + pl;
     double acc[kAdjVals] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int t = 0; t < ntiles; ++t) {
-        const float* p = partials + ((size_t)t * pulses + n) * kAdjVals;
+    if (n < pulses) {
+        for (int t = grp; t < ntiles; t += kSumGroups) {
+            const float* p = partials + ((size_t)t * pulses + n) * kAdjVals;
 #pragma unroll
-        for (int v = 0; v < kAdjVals; ++v) acc[v] += (double)p[v];
+            for (int v = 0; v < kAdjVals; ++v) acc[v] += (double)p[v];
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < kAdjVals; ++v) part[grp][pl][v] = acc[v];
+    __syncthreads();
+    if (grp != 0 || n >= pulses) return;
+#pragma unroll
+    for (int v = 0; v < kAdjVals; ++v) {
+        double s = part[0][pl][v];
+        for (int g = 1; g < kSumGroups; ++g) s += part[g][pl][v];
+        acc[v] = s;
     }
     const double w = weight[n];
     if (grad_pos) {
@@ -1110,7 +1140,7 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
         q.ar = q.ai = 0.0f;
     }
     LeafRec* rec = reinterpret_cast<LeafRec*>(smem);
-    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxChunk * sizeof(LeafRec));
+    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxLeafChunk * sizeof(LeafRec));
     const PulseInputs& in = P.in;
     const float inv_dr = P.inv_drf, Kf = P.Kf;
     for (int c0 = g.a; c0 < g.b;) {
@@ -1243,8 +1273,8 @@ __global__ void __launch_bounds__(kThreads, 3) split_leaf_kernel(SplitParams P, 
                                                                  float2* __restrict__ arena, float2* root_out,
                                                                  int root) {
     extern __shared__ __align__(16) char smem[];
-    __shared__ int s_base[kMaxChunk];
-    __shared__ float s_wt[kMaxChunk];
+    __shared__ int s_base[kMaxLeafChunk];
+    __shared__ float s_wt[kMaxLeafChunk];
     __shared__ int s_nfit;
     leaf_tile(P, nodes, items[blockIdx.x], tables, precs, arena, root_out, root, smem, s_base, s_wt, s_nfit);
 }
@@ -1492,9 +1522,10 @@ int split_window_bins(double radius, double data_dr) {
     return (int)ceil(2.0 * wing) + 4;
 }
 
-int split_chunk_for(int window_bins, int requested) {
-    int ch = requested > 0 ? requested : kMaxChunk;
-    if (ch > kMaxChunk) ch = kMaxChunk;
+int split_chunk_for(int window_bins, int requested, bool leaf) {
+    const int most = leaf ? kMaxLeafChunk : kMaxChunk;
+    int ch = requested > 0 ? requested : most;
+    if (ch > most) ch = most;
     const int fit = kWindowBudget / (window_bins * 32 > 0 ? window_bins * 32 : 32);
     if (ch > fit) ch = fit;
     return ch < 1 ? 1 : ch;
@@ -1591,8 +1622,8 @@ int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat
     }
     note_launches(1);
     if (int st = check_launch("split_lattice_adjoint")) return st;
-    adjoint_sum_kernel<<<grid_blocks(in.pulses, kThreads), kThreads, 0, s>>>(partials, ntiles, in.pulses, in.weight,
-                                                                            grad_pos, grad_phase, grad_weight);
+    adjoint_sum_kernel<<<grid_blocks(in.pulses, kSumPulses), kThreads, 0, s>>>(partials, ntiles, in.pulses, in.weight,
+                                                                              grad_pos, grad_phase, grad_weight);
     note_launches(1);
     return check_launch("adjoint_sum");
 }
@@ -1636,7 +1667,7 @@ int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, cons
                              float2* root_out, int root, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
-    const size_t smem = (size_t)kMaxChunk * sizeof(LeafRec) + (size_t)P.cap * 32;
+    const size_t smem = (size_t)kMaxLeafChunk * sizeof(LeafRec) + (size_t)P.cap * 32;
     if (int st = prepare(split_leaf_kernel, smem)) return st;
     split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const PulseRec*>(precs),
                                                      arena, root_out, root);
@@ -1736,8 +1767,8 @@ __global__ void __launch_bounds__(kThreads, 3) batch_bp_kernel(const BatchScene*
                                                                float2* __restrict__ arena, int* counter) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ int s_base[kMaxChunk];
-    __shared__ float s_wt[kMaxChunk];
+    __shared__ int s_base[kMaxLeafChunk];
+    __shared__ float s_wt[kMaxLeafChunk];
     __shared__ int s_nfit, s_item, s_scene;
     __shared__ __align__(16) BatchScene sc;
     if (threadIdx.x == 0) s_scene = -1;
@@ -1813,7 +1844,8 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     b.has_z = (d.lat.step_row[2] != 0.0 || d.lat.step_col[2] != 0.0) ? 1 : 0;
     b.prec_offset = d.prec_offset;
     memcpy(dst, &b, sizeof(b));
-    return (size_t)kMaxChunk * (d.kind == 0 ? sizeof(Rec) : sizeof(LeafRec)) + (size_t)b.P.cap * 32;
+    return (d.kind == 0 ? (size_t)kMaxChunk * sizeof(Rec) : (size_t)kMaxLeafChunk * sizeof(LeafRec)) +
+           (size_t)b.P.cap * 32;
 }
 
 int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm) {
