@@ -43,7 +43,7 @@ REF_SAMPLE_PIXELS = 131072          # pixels per step of the reference arm (~1 s
 # DRAM bytes (read + write) of one split_lattice_kernel launch on this workload, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum): only the ~920 range bins per pulse that the scene spans
 # are read, so traffic is far below the algorithmic 302 MB.
-NCU_TRAFFIC_BYTES = 31.946752e6 + 2.132224e6
+NCU_TRAFFIC_BYTES = 31.903744e6 + 2.073344e6
 
 
 def parse():
@@ -464,33 +464,53 @@ def main():
     value = world * units * args.steps / (total_ms / 1e3) / 1e9
     image = out.cpu().numpy()
 
-    # End to end through the public API: pinned host inputs -> device -> BP -> host image, every step.
+    # End to end through the public API: every step copies its inputs from pinned host memory to the
+    # device, forms the image (core.backproject_lattice, the C ABI) and reads the image back to the host.
+    # Two buffer sets and a copy stream overlap step i's copies with step i-1's BP.
     host_data = torch.from_numpy(scene.data).pin_memory()
     host_pos = torch.from_numpy(scene.position).pin_memory()
     host_w = torch.from_numpy(scene.weight).pin_memory()
     host_ph = torch.from_numpy(scene.phase).pin_memory()
-    host_out = torch.empty((lat.rows, lat.cols), dtype=torch.complex64).pin_memory()
-    d_data, d_pos, d_w, d_ph = (torch.empty_like(t, device=dev) for t in (host_data, host_pos, host_w, host_ph))
+    host_outs = [torch.empty((lat.rows, lat.cols), dtype=torch.complex64).pin_memory() for _ in range(2)]
+    bufs = [[torch.empty_like(t, device=dev) for t in (host_data, host_pos, host_w, host_ph)] for _ in range(2)]
+    outs = [torch.empty((lat.rows, lat.cols), dtype=torch.complex64, device=dev) for _ in range(2)]
+    copy_stream = torch.cuda.Stream(device=dev)
+    loaded = [torch.cuda.Event() for _ in range(2)]
+    formed = [torch.cuda.Event() for _ in range(2)]
+    freed = [torch.cuda.Event() for _ in range(2)]
+    for ev_ in freed:
+        ev_.record(stream)
 
-    def e2e_step():
-        d_data.copy_(host_data, non_blocking=True)
-        d_pos.copy_(host_pos, non_blocking=True)
-        d_w.copy_(host_w, non_blocking=True)
-        d_ph.copy_(host_ph, non_blocking=True)
-        core.backproject_lattice(d_data, d_pos, d_w, d_ph, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
-                                 scene.range_start, scene.data_dr, scene.k, mode="split", out=out)
-        host_out.copy_(out, non_blocking=True)
+    def e2e_step(i):
+        b = i % 2
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(freed[b])  # step i-2 has finished with buffer set b
+            for d, h in zip(bufs[b], (host_data, host_pos, host_w, host_ph)):
+                d.copy_(h, non_blocking=True)
+            loaded[b].record(copy_stream)
+        stream.wait_event(loaded[b])
+        core.backproject_lattice(*bufs[b], lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                 scene.range_start, scene.data_dr, scene.k, mode="split", out=outs[b])
+        formed[b].record(stream)
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(formed[b])
+            host_outs[b].copy_(outs[b], non_blocking=True)
+            freed[b].record(copy_stream)
 
-    for _ in range(2):
-        e2e_step()
+    for i in range(2):
+        e2e_step(i)
+    torch.cuda.synchronize()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    copy_stream.wait_event(e0)
+    for i in range(args.steps):
+        e2e_step(i)
+    stream.wait_stream(copy_stream)  # the last image is back on the host
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
+    host_out = host_outs[0]
     h2d = sum(t.numel() * t.element_size() for t in (host_data, host_pos, host_w, host_ph))
     d2h = host_out.numel() * host_out.element_size()
 
@@ -582,7 +602,8 @@ def main():
                    "l2": "inputs larger than L2 (268 MB range data per step)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * units / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                "path": "pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), image -> host"},
+                "path": "every step: pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), "
+                        "image -> pinned host; copies on a second stream overlap the previous step's BP"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
                      "kernel": "split_lattice_kernel", "note": f"peak of {peak_kind}; algorithmic bytes "
