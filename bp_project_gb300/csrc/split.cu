@@ -44,7 +44,6 @@ constexpr int kWindowBudget = 68 * 1024;
 // K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
 // error, FFBP leaves 1e-4.
 constexpr double kDirectEnvelope = 8.0;
-constexpr double kLeafEnvelope = 64.0;
 
 struct Rec {
     float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y

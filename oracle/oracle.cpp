@@ -1,7 +1,7 @@
 // CPU oracle for the SAR back-projection path.  TEST INFRASTRUCTURE ONLY:
 // the product (bp_project_gb300) never links, loads or calls this file; only
-// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as a
-// checker and as the timed CPU baseline.
+// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+// FP64 result the GPU path is compared with and as the timed CPU baseline.
 //
 // This is a plain FP64 restatement of the reference's Numba kernels
 // (fast_bp/ffbp.py).  Every function below names the reference lines it

@@ -166,6 +166,42 @@ def test_c0_full_image_vs_fp64_oracle(lib):
     assert rel_err(full, mixed) <= 1e-5
 
 
+@pytest.mark.parametrize("shape,step,tilt,shift", [((37, 45), 0.5, 0.0, 0.0),      # ragged tile edges
+                                                   ((64, 100), 1.3, 0.0, "edge"),  # runs past the range window
+                                                   ((33, 31), 0.7, 0.12, 0.0)])    # tilted (3-D) lattice
+def test_ragged_and_edge_lattices_vs_fp64_oracle(lib, shape, step, tilt, shift):
+    """Lattices that are not tile multiples, that extend beyond the data's range window (pixels
+    with no sample1 support must be exactly the oracle's), and that are not flat."""
+    from bp_project_gb300 import core
+    from oracle import reference as ora
+    sc = _scene("c0", pulses=384, image_side=64)
+    lat = sc.lattice
+    rows, cols = shape
+    if shift == "edge":  # centre the lattice's rows on the far end of the range window
+        far = sc.range_start + (sc.data.shape[1] - 3) * sc.data_dr
+        edge = np.sqrt(far ** 2 - sc.config.altitude ** 2)
+        shift = edge - lat.origin[0] - 0.5 * rows * step
+    origin = (lat.origin[0] + shift, lat.origin[1], 0.0)
+    srow, scol = (step, 0.0, tilt), (0.0, step, 0.0)
+    i = np.arange(rows)[:, None, None]
+    j = np.arange(cols)[None, :, None]
+    pts = (np.array(origin) + i * np.array(srow) + j * np.array(scol)).reshape(-1, 3)
+    _, ref = ora.backproject_points(sc.data, sc.position, pts, sc.range_start, sc.data_dr, sc.k, sc.weight, sc.phase,
+                                    c128=True)
+    args = [_dev(a, dt) for a, dt in ((sc.data, torch.complex64), (sc.position, torch.float64),
+                                      (sc.weight, torch.float64), (sc.phase, torch.float64))]
+    for mode, tol in (("split", 1e-5), ("fp64", 1e-6)):
+        out = core.backproject_lattice(*args, origin, srow, scol, rows, cols, sc.range_start, sc.data_dr, sc.k,
+                                       mode=mode).cpu().numpy().ravel()
+        zero = np.abs(ref) == 0
+        if shift:
+            assert zero.any() and (~zero).any()  # part of the lattice lies outside the range window
+        assert np.all(out[zero] == 0)
+        err = rel_err(ref, out)
+        print(f"{shape} step {step} tilt {tilt} shift {shift} {mode}: {err:.2e}")
+        assert err <= tol
+
+
 def test_evaluate_lattice_matches_points_path(lib):
     """Split-precision evaluate onto the 512^2 ground lattice vs the FP64-geometry points kernel."""
     from bp_project_gb300 import core
