@@ -380,7 +380,7 @@ def run_batch(args, rank):
                    "l2": "inputs far larger than L2 (%.1f GB of range data)" % (
                        sum(sc.data.numel() * 8 for sc in items) / 1e9)},
         "scenes_per_s": len(items) / (batch_ms / 1e3),
-        "graph": "one CUDA graph per batch: %d launches (memset, 3 FFBP prologues, 1 persistent BP, %d persistent "
+        "graph": "one CUDA graph per batch: %d launches (memset, 3 FFBP prologues, persistent direct and leaf launches, %d persistent "
                  "merge levels)" % (batch.launch_count, batch.info["max_height"]),
         "batch_info": batch.info, "autotune": {str(k): list(v) for k, v in choices.items()},
         "autotune_blocks_per_sm": {"chosen": blocks, "ms": block_timings},

@@ -20,7 +20,7 @@ import torch
 from .batch import DirectScene, SceneBatch
 
 TILE_LCS = (3, 4, 5)
-CHUNKS = (8, 16, 32)
+CHUNKS = (16, 32, 64)
 BLOCKS_PER_SM = (2, 3)
 DEFAULT_CACHE = Path(os.environ.get("SARBP_AUTOTUNE_CACHE", Path(__file__).resolve().parent / ".autotune.json"))
 

@@ -5,8 +5,8 @@
 // its nodes, tiles, tables, pulse records, child records and node images are then
 // re-based into batch-wide arrays, so one set of launches covers all scenes:
 //   memset(queue counters) -> tables -> leaf pulse records -> merge child records
-//   -> one persistent BP launch over every direct tile and FFBP leaf tile
-//      (largest first, so the queue drains evenly)
+//   -> one persistent launch over every direct tile (largest first, so the queue drains
+//      evenly) and one over every FFBP leaf tile
 //   -> one persistent merge launch per tree height over every scene's nodes of
 //      that height.
 // Items are independent within a launch, and heights are separated by launches, so
@@ -33,8 +33,9 @@ struct sarbp_batch {
     std::vector<int> level_begin, level_count;  // merge heights 1..max_height at index h - 1
     int max_height = 0, max_dim = 1;
     long long table_entries = 0, pulse_records = 0;
-    size_t smem = 0;
-    int bp_blocks = 1, merge_blocks = 1;
+    size_t direct_smem = 0, leaf_smem = 0;
+    int n_direct = 0;             // bp_items[0, n_direct) are direct tiles, the rest leaf tiles
+    int bp_blocks = 1, leaf_blocks = 1, merge_blocks = 1;
     int direct_scenes = 0, ffbp_scenes = 0;
     double pixel_pulses = 0.0;    // direct-equivalent work: pixels x pulses summed over scenes
     size_t scene_off = 0, node_off = 0, bp_off = 0, merge_off = 0, leaf_off = 0, counter_off = 0, table_off = 0,
@@ -187,12 +188,21 @@ int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks
             ++b->ffbp_scenes;
         }
         const size_t smem = split_batch_pack_scene(d, b->scenes.data() + scene_bytes * i);
-        b->smem = std::max(b->smem, smem);
+        if (s.kind == SARBP_BATCH_DIRECT)
+            b->direct_smem = std::max(b->direct_smem, smem);
+        else
+            b->leaf_smem = std::max(b->leaf_smem, smem);
     }
-    // Largest items first (stable: scenes and tiles keep their order among equals).
+    // Direct tiles first, largest first (stable: scenes and tiles keep their order among equals),
+    // then the leaf tiles.
     std::vector<int> order(b->bp_items.size());
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bp_cost[x] > bp_cost[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const bool dx = b->bp_items[x].node < 0, dy = b->bp_items[y].node < 0;
+        if (dx != dy) return dx;
+        return bp_cost[x] > bp_cost[y];
+    });
+    for (const TileItem& it : b->bp_items) b->n_direct += it.node < 0 ? 1 : 0;
     std::vector<TileItem> sorted(order.size());
     for (size_t t = 0; t < order.size(); ++t) sorted[t] = b->bp_items[order[t]];
     b->bp_items.swap(sorted);
@@ -206,23 +216,28 @@ int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks
         return fail(SARBP_ERR_PLAN, "batch too large");
     }
     // Persistent grids: every resident CTA slot of the GPU (or blocks_per_sm per SM).
-    int dev = 0, sms = 1, bp_occ = 1, merge_occ = 1;
+    int dev = 0, sms = 1, direct_occ = 1, leaf_occ = 1, merge_occ = 1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) {
         delete b;
         return fail(SARBP_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
     }
-    if (int st = split_batch_occupancy(b->smem, &bp_occ, &merge_occ)) {
+    const size_t min_smem = 1024;
+    if (int st = split_batch_occupancy(std::max(b->direct_smem, min_smem), std::max(b->leaf_smem, min_smem),
+                                       &direct_occ, &leaf_occ, &merge_occ)) {
         delete b;
         return st;
     }
-    if (bp_occ < 1) {
+    if (direct_occ < 1 || leaf_occ < 1) {
         delete b;
-        return fail(SARBP_ERR_VALUE, "batch: %zu bytes of shared memory per CTA do not fit an SM", b->smem);
+        return fail(SARBP_ERR_VALUE, "batch: %zu / %zu bytes of shared memory per CTA do not fit an SM",
+                    b->direct_smem, b->leaf_smem);
     }
-    const int per_sm = blocks_per_sm ? std::min(blocks_per_sm, bp_occ) : bp_occ;
-    b->bp_blocks = std::max(1, std::min((int)b->bp_items.size(), sms * per_sm));
+    const int n_leaf = (int)b->bp_items.size() - b->n_direct;
+    const int per_sm = blocks_per_sm ? std::min(blocks_per_sm, direct_occ) : direct_occ;
+    b->bp_blocks = std::max(1, std::min(b->n_direct, sms * per_sm));
+    b->leaf_blocks = std::max(1, std::min(n_leaf, sms * leaf_occ));
     b->merge_blocks = std::max(1, sms * std::max(1, merge_occ));
     // Workspace layout.
     b->scene_off = 0;
@@ -231,12 +246,12 @@ int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks
     b->merge_off = b->bp_off + align_up(sizeof(TileItem) * b->bp_items.size());
     b->leaf_off = b->merge_off + align_up(sizeof(TileItem) * b->merge_items.size());
     b->counter_off = b->leaf_off + align_up(sizeof(int) * b->leaves.size());
-    b->table_off = b->counter_off + align_up(sizeof(int) * (1 + b->max_height));
+    b->table_off = b->counter_off + align_up(sizeof(int) * (2 + b->max_height));
     b->prec_off = b->table_off + align_up(sizeof(float4) * (size_t)b->table_entries);
     b->crec_off = b->prec_off + align_up(split_ffbp_pulse_record_bytes() * (size_t)b->pulse_records);
     b->arena_off = b->crec_off + align_up(split_ffbp_child_record_bytes() * 2 * b->merge_items.size());
     b->total = b->arena_off + arena;
-    b->launches = 1 + (b->ffbp_scenes ? 3 : 0) + 1 + b->max_height;
+    b->launches = 1 + (b->ffbp_scenes ? 4 : 0) + (b->direct_scenes ? 1 : 0) + b->max_height;
     *batch_out = b;
     return SARBP_OK;
 }
@@ -300,21 +315,25 @@ int sarbp_batch_execute(const sarbp_batch* batch, void* stream) {
     void* precs = base + batch->prec_off;
     char* crecs = base + batch->crec_off;
     float2* arena = reinterpret_cast<float2*>(base + batch->arena_off);
-    cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(int) * (1 + batch->max_height), s);
+    cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(int) * (2 + batch->max_height), s);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "batch counters: %s", cudaGetErrorString(e));
     int st = SARBP_OK;
     if (batch->ffbp_scenes)
         st = launch_split_batch_prologue(scenes, nodes, (int)batch->nodes.size(), batch->max_dim, leaves,
                                          (int)batch->leaves.size(), merge_items, (int)batch->merge_items.size(),
                                          tables, precs, crecs, arena, s);
+    const int n_leaf = (int)batch->bp_items.size() - batch->n_direct;
     if (st == SARBP_OK)
-        st = launch_split_batch_bp(scenes, nodes, bp_items, (int)batch->bp_items.size(), tables, precs, arena,
-                                   counters, batch->bp_blocks, batch->smem, s);
+        st = launch_split_batch_direct(scenes, bp_items, batch->n_direct, counters, batch->bp_blocks,
+                                       batch->direct_smem, s);
+    if (st == SARBP_OK)
+        st = launch_split_batch_leaves(scenes, nodes, bp_items + batch->n_direct, n_leaf, tables, precs, arena,
+                                       counters + 1, batch->leaf_blocks, batch->leaf_smem, s);
     const size_t crec_size = split_ffbp_child_record_bytes();
     for (int h = 1; h <= batch->max_height && st == SARBP_OK; ++h) {
         const int first = batch->level_begin[h - 1], count = batch->level_count[h - 1];
         st = launch_split_batch_merges(scenes, nodes, merge_items + first, count, tables,
-                                       crecs + 2 * (size_t)first * crec_size, arena, counters + h,
+                                       crecs + 2 * (size_t)first * crec_size, arena, counters + 1 + h,
                                        std::min(batch->merge_blocks, std::max(1, count)), s);
     }
     return st;

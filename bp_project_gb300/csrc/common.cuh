@@ -182,13 +182,16 @@ struct BatchSceneDesc {
 size_t split_batch_scene_bytes();
 // Writes the device form of `d` to dst; returns the dynamic shared memory its tiles need.
 size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst);
-int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm);
+int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_sm, int* leaf_per_sm,
+                          int* merge_per_sm);
 int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int n_nodes, int max_dim,
                                 const int* leaves, int n_leaves, const TileItem* merge_items, int n_merge_items,
                                 float4* tables, void* precs, void* crecs, float2* arena, cudaStream_t s);
-int launch_split_batch_bp(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
-                          const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
-                          size_t smem, cudaStream_t s);
+int launch_split_batch_direct(const void* scenes, const TileItem* items, int nitems, int* counter, int blocks,
+                              size_t smem, cudaStream_t s);
+int launch_split_batch_leaves(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                              const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
+                              size_t smem, cudaStream_t s);
 int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
                               const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
                               cudaStream_t s);

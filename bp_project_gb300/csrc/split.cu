@@ -1758,17 +1758,13 @@ __device__ __forceinline__ void load_scene(const BatchScene* __restrict__ scenes
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads, 3) batch_bp_kernel(const BatchScene* __restrict__ scenes,
-                                                               const PolarDesc* __restrict__ nodes,
-                                                               const TileItem* __restrict__ items, int nitems,
-                                                               const float4* __restrict__ tables,
-                                                               const PulseRec* __restrict__ precs,
-                                                               float2* __restrict__ arena, int* counter) {
+// Direct tiles of every direct scene (flat lattices only, checked when the batch is created).
+__global__ void __launch_bounds__(kThreads, 3) batch_direct_kernel(const BatchScene* __restrict__ scenes,
+                                                                   const TileItem* __restrict__ items, int nitems,
+                                                                   int* counter) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ int s_base[kMaxLeafChunk];
-    __shared__ float s_wt[kMaxLeafChunk];
-    __shared__ int s_nfit, s_item, s_scene;
+    __shared__ int s_item, s_scene;
     __shared__ __align__(16) BatchScene sc;
     if (threadIdx.x == 0) s_scene = -1;
     for (;;) {
@@ -1779,10 +1775,32 @@ __global__ void __launch_bounds__(kThreads, 3) batch_bp_kernel(const BatchScene*
             load_scene(scenes, it.pad, sc);
             if (threadIdx.x == 0) s_scene = it.pad;
         }
-        if (sc.kind == 0)  // flat lattices only (checked when the batch is created)
-            lattice_tile<false>(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
-        else
-            leaf_tile(sc.P, nodes, it, tables, precs + sc.prec_offset, arena, nullptr, -1, smem, s_base, s_wt, s_nfit);
+        lattice_tile<false>(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
+    }
+}
+
+// Leaf tiles of every FFBP scene.
+__global__ void __launch_bounds__(kThreads, 3) batch_leaf_kernel(const BatchScene* __restrict__ scenes,
+                                                                 const PolarDesc* __restrict__ nodes,
+                                                                 const TileItem* __restrict__ items, int nitems,
+                                                                 const float4* __restrict__ tables,
+                                                                 const PulseRec* __restrict__ precs,
+                                                                 float2* __restrict__ arena, int* counter) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ int s_base[kMaxLeafChunk];
+    __shared__ float s_wt[kMaxLeafChunk];
+    __shared__ int s_nfit, s_item, s_scene;
+    __shared__ __align__(16) BatchScene sc;
+    if (threadIdx.x == 0) s_scene = -1;
+    for (;;) {
+        const int idx = next_item(counter, s_item);
+        if (idx >= nitems) return;
+        const TileItem it = items[idx];
+        if (it.pad != s_scene) {
+            load_scene(scenes, it.pad, sc);
+            if (threadIdx.x == 0) s_scene = it.pad;
+        }
+        leaf_tile(sc.P, nodes, it, tables, precs + sc.prec_offset, arena, nullptr, -1, smem, s_base, s_wt, s_nfit);
     }
 }
 
@@ -1847,13 +1865,17 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
            (size_t)b.P.cap * 32;
 }
 
-int split_batch_occupancy(size_t smem, int* bp_blocks_per_sm, int* merge_blocks_per_sm) {
-    if (int st = prepare(batch_bp_kernel, smem)) return st;
+int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_sm, int* leaf_per_sm,
+                          int* merge_per_sm) {
+    if (int st = prepare(batch_direct_kernel, direct_smem)) return st;
+    if (int st = prepare(batch_leaf_kernel, leaf_smem)) return st;
     if (int st = prepare(batch_merge_kernel, merge_smem())) return st;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bp_blocks_per_sm, batch_bp_kernel, kThreads, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(direct_per_sm, batch_direct_kernel, kThreads,
+                                                                  direct_smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_blocks_per_sm, batch_merge_kernel, kThreads,
-                                                          merge_smem());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(leaf_per_sm, batch_leaf_kernel, kThreads, leaf_smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_per_sm, batch_merge_kernel, kThreads, merge_smem());
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
@@ -1882,15 +1904,25 @@ int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int 
     return SARBP_OK;
 }
 
-int launch_split_batch_bp(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
-                          const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
-                          size_t smem, cudaStream_t s) {
+int launch_split_batch_direct(const void* scenes, const TileItem* items, int nitems, int* counter, int blocks,
+                              size_t smem, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
-    if (int st = prepare(batch_bp_kernel, smem)) return st;
-    batch_bp_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes, items, nitems,
-                                                   tables, reinterpret_cast<const PulseRec*>(precs), arena, counter);
+    if (int st = prepare(batch_direct_kernel, smem)) return st;
+    batch_direct_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), items, nitems,
+                                                       counter);
     note_launches(1);
-    return check_launch("batch_bp");
+    return check_launch("batch_direct");
+}
+
+int launch_split_batch_leaves(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
+                              const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
+                              size_t smem, cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    if (int st = prepare(batch_leaf_kernel, smem)) return st;
+    batch_leaf_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes, items, nitems,
+                                                     tables, reinterpret_cast<const PulseRec*>(precs), arena, counter);
+    note_launches(1);
+    return check_launch("batch_leaves");
 }
 
 int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,

@@ -78,7 +78,7 @@ def test_batch_equals_single_scene_paths(small_batch):
         kinds.append(type(sc).__name__)
     assert "DirectScene" in kinds and "FFBPScene" in kinds
     print(batch.info, "launches", batch.launch_count)
-    assert batch.launch_count == 1 + 3 + 1 + batch.info["max_height"]
+    assert batch.launch_count == 1 + 4 + 1 + batch.info["max_height"]  # memset, prologues + leaves, direct, merges
     # graph capture + replay reproduce the eager result
     first = [o.clone() for o in batch.outputs]
     for o in batch.outputs:
@@ -98,7 +98,7 @@ def test_batch_tile_shapes_and_chunks(small_batch):
     from bp_project_gb300.batch import DirectScene, SceneBatch
     direct = [sc for sc in small_batch if isinstance(sc, DirectScene)][:2]
     ref = [single(sc) for sc in direct]
-    for lc, ch in ((3, 8), (4, 16), (5, 8)):
+    for lc, ch in ((3, 8), (4, 16), (5, 8), (5, 64)):
         cands = [DirectScene(**{**sc.__dict__, "tile_lc": lc, "chunk_pulses": ch, "out": None}) for sc in direct]
         batch = SceneBatch(cands, blocks_per_sm=2)
         batch.execute()
