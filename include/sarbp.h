@@ -186,10 +186,10 @@ int sarbp_backproject_lattice_adjoint(const float* data, int pulses, int samples
 
 /* Many independent scenes of uneven pulse and pixel counts formed together:
  * direct split-precision BP onto a flat lattice, or split-precision FFBP of a
- * plan (the nodes sarbp_ffbp_plan_create takes).  All scenes' direct tiles and
- * FFBP leaf tiles run in one persistent launch that takes work from a queue,
- * largest items first; FFBP merges run as one persistent launch per tree
- * height across all scenes.  Each scene's output equals the single-scene entry
+ * plan (the nodes sarbp_ffbp_plan_create takes).  All scenes' direct tiles run
+ * in one persistent launch that takes work from a queue, largest items first,
+ * and all FFBP leaf tiles in another; FFBP merges run as one persistent launch
+ * per tree height across all scenes.  Each scene's output equals the single-scene entry
  * point's (sarbp_backproject_lattice / sarbp_ffbp_execute, split mode) bit for
  * bit when the tile shape is the same.  Inputs and outputs are bound at
  * creation; execute never synchronises or allocates and is graph-capturable.
