@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ffbp", action="store_true")
+    ap.add_argument("--no-autofocus", action="store_true")
     ap.add_argument("--workload", choices=("direct", "autofocus", "batch"), default="direct")
     ap.add_argument("--scenes", type=int, default=64)
     return ap.parse_args()
@@ -246,6 +247,37 @@ def autofocus_case(dev, walk_sigma):
                       "gpu_pga": e_gpu_pga, "entropy_autofocus": full.entropy},
         "speedup_vs_reference_pga": ref_s / t_target,
     }
+
+
+def autofocus_rates(dev):
+    """Autofocus iterations per second on the 2048-pulse scene (GPU only; the CPU comparison is
+    ``--workload autofocus``): the reference's phase-gradient loop (FFBP + target picking + update per
+    iteration) and the gradient entropy autofocus (one forward + adjoint BP per evaluation)."""
+    import torch
+
+    from bp_project_gb300.autofocus import entropy_autofocus, phase_gradient_autofocus
+    sc, data, nav, weight, phase = autofocus_scene(str(dev))
+    cfg, lat = sc.config, sc.lattice
+    d, w, ph = (torch.from_numpy(a).to(dev) for a in (data, weight, phase))
+    nav_t = torch.from_numpy(nav).to(dev)
+    pga = dict(side=1, leaf_size=64, range_spacing=0.5, angular_oversample=2.0, weight=weight)
+    phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent, cfg.prf, cutoffs=(12,), **pga)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, records = phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent, cfg.prf, **pga)
+    torch.cuda.synchronize()
+    pga_s = time.perf_counter() - t0
+    geo = (tuple(lat.origin), tuple(lat.step_row), tuple(lat.step_col), lat.rows, lat.cols, sc.range_start,
+           sc.data_dr, sc.k)
+    entropy_autofocus(d, nav_t, w, ph, *geo, steps=2)
+    torch.cuda.synchronize()
+    res = entropy_autofocus(d, nav_t, w, ph, *geo, steps=20)
+    per_eval = res.history[-1][0] / res.evaluations
+    return {"pga_iters_per_s": len(records) / pga_s, "pga_iterations": len(records),
+            "entropy_evals_per_s": 1.0 / per_eval, "entropy_evaluations": res.evaluations,
+            "entropy_after": res.entropy,
+            "workload": "2048 pulses x 4096 bins, 1024^2 lattice; PGA: FFBP (leaf 64) + 12x12 target picks + "
+                        "estimate_update per iteration; entropy: forward + adjoint BP per L-BFGS evaluation"}
 
 
 def run_autofocus(args, rank):
@@ -577,6 +609,9 @@ def main():
             "ffbp_vs_direct_err": float(np.linalg.norm(g - image) / np.linalg.norm(image)),
         })
         prog.close()
+
+    if rank == 0 and not args.no_autofocus:
+        extra["autofocus"] = autofocus_rates(dev)
 
     if rank != 0:
         if world > 1:

@@ -10,11 +10,16 @@
 // filtered again over the reversed output starting from zi * its first
 // sample, and the extension is cut off.  The extension is formed in complex64
 // arithmetic like the reference's (its input is complex64); the filter runs
-// in FP64 with explicit roundings (no contraction).
+// in FP64 with explicit roundings (no contraction; on GB300 separate FP64
+// multiplies and adds also run faster than fused ones here).
 //
-// One thread per (row, real/imag) channel: the recursion is serial along the
-// pulses, the rows are independent.  The forward pass is kept in a
-// time-major workspace so that a warp's 32 channels touch consecutive words.
+// The recursion is serial along the pulses and the rows are independent.  One warp
+// per row: its lanes build the odd-extended row in shared memory with coalesced
+// loads, then lanes 0 and 1 (real, imaginary) run the forward pass into shared
+// memory and the backward pass out to the result, so every step of the recursion
+// reads shared memory instead of waiting on a global load.  Rows too long for
+// shared memory use one thread per channel with the forward pass in a time-major
+// global workspace.
 #include "common.cuh"
 
 namespace sarbp {
@@ -98,6 +103,67 @@ __global__ void sosfiltfilt_kernel(const float* __restrict__ x, int rows, int n,
     }
 }
 
+constexpr size_t kRowSmemLimit = 200 * 1024;
+
+size_t row_smem(int n, int padlen) { return (size_t)(n + 2 * padlen) * (sizeof(double2) + sizeof(float2)); }
+
+__global__ void __launch_bounds__(32) sosfiltfilt_row_kernel(const float* __restrict__ x, int n,
+                                                             const double* __restrict__ sos,
+                                                             const double* __restrict__ zi, int sections, int padlen,
+                                                             double* __restrict__ y) {
+    extern __shared__ __align__(16) char smem[];
+    const int row = blockIdx.x, lane = threadIdx.x;
+    const int m = n + 2 * padlen;
+    double2* fwd = reinterpret_cast<double2*>(smem);
+    float2* ext = reinterpret_cast<float2*>(smem + (size_t)m * sizeof(double2));
+    const float* xr = x + (size_t)row * n * 2;
+    for (int i = lane; i < m; i += 32) ext[i] = make_float2(extended(xr, n, padlen, i, 0), extended(xr, n, padlen, i, 1));
+    __syncwarp();
+    if (lane < 2) {
+        const int comp = lane;
+        Biquads f;
+        f.sections = sections;
+        double zs0[kMaxSections], zs1[kMaxSections];
+#pragma unroll
+        for (int s = 0; s < kMaxSections; ++s) {
+            if (s < sections) {
+                f.b0[s] = sos[6 * s];
+                f.b1[s] = sos[6 * s + 1];
+                f.b2[s] = sos[6 * s + 2];
+                f.a1[s] = sos[6 * s + 4];  // a0 == 1 (checked by the caller)
+                f.a2[s] = sos[6 * s + 5];
+                zs0[s] = zi[2 * s];
+                zs1[s] = zi[2 * s + 1];
+            }
+        }
+        const float* e = reinterpret_cast<const float*>(ext) + comp;
+        double* fw = reinterpret_cast<double*>(fwd) + comp;
+        const double first = (double)e[0];
+#pragma unroll
+        for (int s = 0; s < kMaxSections; ++s) {
+            if (s < sections) {
+                f.z0[s] = __dmul_rn(zs0[s], first);
+                f.z1[s] = __dmul_rn(zs1[s], first);
+            }
+        }
+        for (int i = 0; i < m; ++i) fw[2 * i] = f.step((double)e[2 * i]);
+        const double last = fw[2 * (m - 1)];
+#pragma unroll
+        for (int s = 0; s < kMaxSections; ++s) {
+            if (s < sections) {
+                f.z0[s] = __dmul_rn(zs0[s], last);
+                f.z1[s] = __dmul_rn(zs1[s], last);
+            }
+        }
+        double* yr = y + (size_t)row * n * 2 + comp;
+        for (int i = m - 1; i >= 0; --i) {
+            const double v = f.step(fw[2 * i]);
+            const int j = i - padlen;
+            if (j >= 0 && j < n) yr[2 * j] = v;
+        }
+    }
+}
+
 }  // namespace
 
 size_t sosfiltfilt_workspace(int rows, int n, int padlen) {
@@ -106,6 +172,17 @@ size_t sosfiltfilt_workspace(int rows, int n, int padlen) {
 
 int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,
                        double* y, double* ws, cudaStream_t s) {
+    const size_t smem = row_smem(n, padlen);
+    if (smem <= kRowSmemLimit) {
+        if (smem > 48 * 1024) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(sosfiltfilt_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+        }
+        sosfiltfilt_row_kernel<<<rows, 32, smem, s>>>(x, n, sos, zi, sections, padlen, y);
+        note_launches(1);
+        return check_launch("sosfiltfilt");
+    }
     const int channels = 2 * rows;
     const int block = 64;
     sosfiltfilt_kernel<<<grid_blocks(channels, block), block, 0, s>>>(x, rows, n, sos, zi, sections, padlen, y, ws);

@@ -11,7 +11,10 @@ lattice), ``ffbp`` (level-batched FFBP + split evaluation onto the lattice),
 ``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice),
 ``adjoint`` (forward + adjoint of lattice BP, the entropy autofocus step),
 ``range`` (range compression of the scene's data treated as raw echoes),
-``batch`` (a small uneven scene batch through the persistent kernels).
+``batch`` (a small uneven scene batch through the persistent kernels),
+``all`` (every product kernel once on a small scene: direct BP in all modes on
+lattice, polar grid and points, FFBP, evaluation, target contributions, the
+LUT probe, adjoint, range compression, I/Q decode, phase-history filter).
 Prints one JSON line with event timings (not for benchmarking under a
 profiler: bench.py is the benchmark).
 """
@@ -26,9 +29,58 @@ from . import build, core, scenes
 from .gpu_backend import build_ffbp_plan
 
 
+def _all_kernels(scene, data, pos, wt, ph, dev):
+    """One call of every product kernel on the scene (small scenes keep this to tens of ms)."""
+    import numpy as np
+
+    from .autofocus import butter_lowpass, image_entropy, sosfiltfilt
+    from .autograd import backproject_lattice
+    from .sar_io import range_compress
+    cfg, lat = scene.config, scene.lattice
+    plan = build_ffbp_plan(scene.position, cfg.fc, scene.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    progs = {m: core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode=m, device=dev)
+             for m in ("split", "mixed")}
+    grid = plan.grid()
+    from .ffbp import morton_order
+    sample = lat.take(np.arange(0, lat.rows * lat.cols, 7))
+    pts = torch.from_numpy(np.ascontiguousarray(sample[morton_order(sample)])).to(dev)  # as ffbp.backproject_points
+    targets = torch.from_numpy(scene.targets).to(dev)
+    lut = core.fill_range_phase_lut(data.shape[1], scene.range_start, scene.data_dr, scene.k, device=dev)
+    frames = torch.zeros((64, 160 + 4 * data.shape[1] + 32), dtype=torch.uint8, device=dev)
+    from . import _native as nat
+    decoded = torch.empty((64, data.shape[1]), dtype=torch.complex64, device=dev)
+
+    def run():
+        for mode in ("split", "fp32", "mixed", "fp64"):
+            rows = lat.rows if mode in ("split", "fp32") else 32
+            core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, rows, lat.cols,
+                                     scene.range_start, scene.data_dr, scene.k, mode=mode)
+        small = core.Grid(grid.origin, grid.r0, grid.dr, min(grid.nr, 256), grid.u0, grid.du, min(grid.nu, 256),
+                          grid.side)
+        for mode in ("split", "mixed"):
+            core.direct_polar(data, pos, wt, ph, small, scene.range_start, scene.data_dr, scene.k, mode=mode)
+            core.backproject_points(data, pos, wt, ph, pts, scene.range_start, scene.data_dr, scene.k, mode=mode)
+        core.direct_polar_lut(data, pos, wt, ph, small, scene.range_start, scene.data_dr, scene.k, lut)
+        for m, prog in progs.items():
+            polar = prog.execute(data, pos, wt, ph, scene.range_start, scene.data_dr, scene.k)
+        core.evaluate_lattice(polar, grid, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols, scene.k)
+        core.evaluate_image(polar, grid, pts, scene.k)
+        contrib = core.target_contributions(data, pos, targets, scene.range_start, scene.data_dr, scene.k)
+        sosfiltfilt(contrib, butter_lowpass(12.0, cfg.prf))
+        p = pos.clone().requires_grad_()
+        image_entropy(backproject_lattice(data, p, wt, ph, lat.origin, lat.step_row, lat.step_col, lat.rows,
+                                          lat.cols, scene.range_start, scene.data_dr, scene.k)).backward()
+        range_compress(data, tp=1e-6, bandwidth=cfg.bandwidth, fs=cfg.fs, oversample=2)
+        nat.check(nat.load().sarbp_decode_iq(core._ptr(frames), 64, frames.shape[1], 160, data.shape[1],
+                                             core._ptr(decoded), core.stream_handle()), "decode_iq")
+    return run
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=("direct", "ffbp", "plain", "adjoint", "range", "batch"), default="direct")
+    ap.add_argument("--workload", choices=("direct", "ffbp", "plain", "adjoint", "range", "batch", "all"),
+                    default="direct")
     ap.add_argument("--config", default="c1")
     ap.add_argument("--pulses", type=int, default=None, help="scale the scene to this many pulses")
     ap.add_argument("--side", type=int, default=None, help="scale the ground image to side x side pixels")
@@ -58,6 +110,9 @@ def main(argv=None):
             core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, rows, lat.cols,
                                      scene.range_start, scene.data_dr, scene.k, mode=mode, out=out)
         units = rows * lat.cols * cfg.pulses
+    elif args.workload == "all":
+        run = _all_kernels(scene, data, pos, wt, ph, dev)
+        units = lat.rows * lat.cols * cfg.pulses
     elif args.workload == "adjoint":
         from .autofocus import image_entropy
         from .autograd import backproject_lattice
