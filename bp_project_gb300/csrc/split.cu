@@ -72,6 +72,7 @@ struct TileShared {
     float wt[kMaxChunk];
     int nfit;
     int nfit_w[2];              // fitting pulses among each record warp's 32
+    unsigned miss_w[2];         // pulses of each record warp that cannot be staged (bit per lane)
     int wsum;                   // window entries of record warp 0's pulses
 };
 
@@ -98,6 +99,8 @@ struct SplitParams {
     // Precision envelope of the FP32 eps term: the fast path needs K rho^2 / R <= envelope
     // (the FP32 error of eps is ~2.5e-7 * rho^2 / R metres, i.e. ~2.5e-7 * envelope turns).
     double envelope;
+    // Two-float (hi + lo) copies for the FP32 fallback of pulses outside the envelope.
+    float Kh, Kl, rsh, rsl, idrh, idrl;
 };
 
 struct Job {
@@ -513,42 +516,133 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
 // FP64 per-sample evaluation of one pixel over pulses [c0, c0 + chn): the
 // fallback for a pulse whose range window does not fit the staged bins.
 // Everything is passed by value so the caller's pixel state stays in registers.
-__device__ __noinline__ float2 slow_pixel(const float2* __restrict__ data, int samples, const double* __restrict__ pos,
-                                          const double* __restrict__ weight, const double* __restrict__ phase,
-                                          double range_start, double inv_dr, double K, double x, double y, double z,
-                                          float psi, int c0, int chn) {
-    float ar = 0.0f, ai = 0.0f;
-    for (int n = c0; n < c0 + chn; ++n) {
-        const double vx = x - pos[3 * n], vy = y - pos[3 * n + 1], vz = z - pos[3 * n + 2];
-        const double d = sqrt(vx * vx + vy * vy + vz * vz);
-        const double t = K * d + phase[n] * kInvTwoPi;
-        const float tot = (float)(t - rint(t)) + psi;
-        const float ang = (tot - round_magic(tot)) * kTwoPiF;
-        const double qq = (d - range_start) * inv_dr;
-        const double fl = floor(qq);
-        if (!(fl >= 1.0 && fl <= (double)(samples - 3))) continue;
-        const int i = (int)fl;
-        const float2* row = data + (size_t)n * samples;
-        float w[4];
-        lagrange_centred((float)(qq - fl - 0.5), w);
-        float vr = 0.0f, vi = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const float2 v = __ldg(row + i + b - 1);
-            vr = fmaf(w[b], v.x, vr);
-            vi = fmaf(w[b], v.y, vi);
-        }
-        const float a = (float)weight[n];
-        float sn, cs;
-        __sincosf(ang, &sn, &cs);
-        ar = fmaf(a * vr, cs, fmaf(-a * vi, sn, ar));
-        ai = fmaf(a * vr, sn, fmaf(a * vi, cs, ai));
-    }
-    return make_float2(ar, ai);
+// ---- two-float arithmetic (unevaluated sums hi + lo of two FP32 numbers) ----------------
+//
+// Error-free transformations (Knuth's two-sum, the FMA form of Dekker's product) give about
+// 44 significant bits in FP32 arithmetic, which runs at full rate where GB300's FP64 does not.
+// They carry pulses that fall outside the split path's precision envelope.
+struct FF {
+    float h, l;
+};
+
+__device__ __forceinline__ FF ff_norm(float s, float e) {  // |s| >= |e|
+    const float h = s + e;
+    return FF{h, e - (h - s)};
 }
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb);
+    return ff_norm(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.h, -p);
+    return ff_norm(p, fmaf(a.h, b.l, fmaf(a.l, b.h, e)));
+}
+__device__ __forceinline__ FF ff_sqr(FF a) {
+    const float p = a.h * a.h;
+    const float e = fmaf(a.h, a.h, -p);
+    return ff_norm(p, fmaf(2.0f * a.h, a.l, e));
+}
+// sqrt by one Newton step on the FP32 root: s + (a - s^2) / (2 s).
+__device__ __forceinline__ FF ff_sqrt(FF a) {
+    const float s = __fsqrt_rn(a.h);
+    const float p = s * s;
+    const float e = fmaf(s, s, -p);
+    const float r = ((a.h - p) - e) + a.l;
+    return ff_norm(s, r * (0.5f / s));
+}
+
+// Per (tile, pulse) data of a pulse the fast path cannot stage: the FP64 vector from the
+// antenna to the tile centre as two-float components, the pulse phase in turns, the weight.
+struct SlowRec {
+    float4 a;  // w.x hi, w.x lo, w.y hi, w.y lo
+    float4 b;  // w.z hi, w.z lo, phase / 2pi reduced to [-1/2, 1/2], weight
+};
+
+// Sum over pulses [c0, c0 + n) of one pixel's contributions in two-float geometry.  Out of
+// line (and the pixel by value) so that the rarely taken fallback does not add registers
+// to the kernels' fast path.
+__device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* srec, int n, int c0, float dxh,
+                                          float dxl, float dyh, float dyl, float dzh, float dzl, float psi);
+
+// Dynamic shared memory of the chunk kernels: [records | windows]; the two-float records of
+// a chunk that stages no window live at the start of the window space.
+__host__ __device__ constexpr size_t window_offset() { return (size_t)kMaxChunk * sizeof(Rec); }
+
+__device__ __forceinline__ void split2(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+// Range-sample value and its derivative for a pixel at offset delta from the tile centre,
+// pulse record sr, in two-float geometry: returns false when the taps leave the row.
+struct SlowSample {
+    float vr, vi, dvr, dvi;  // sample1 value and d/dq
+    float ang;               // phase (radians, reduced)
+    float ex, ey, ez;        // unit vector pulse -> pixel
+    float d;                 // range (m, FP32)
+};
+
+template <bool DERIV>
+__device__ __forceinline__ bool slow_sample(const SplitParams& P, const SlowRec& sr, const float2* __restrict__ row,
+                                            const Pix& q, float psi, SlowSample& o) {
+    const FF vx = ff_add(FF{sr.a.x, sr.a.y}, FF{q.dxh, q.dxl});
+    const FF vy = ff_add(FF{sr.a.z, sr.a.w}, FF{q.dyh, q.dyl});
+    const FF vz = ff_add(FF{sr.b.x, sr.b.y}, FF{q.dzh, q.dzl});
+    const FF d = ff_sqrt(ff_add(ff_add(ff_sqr(vx), ff_sqr(vy)), ff_sqr(vz)));
+    const FF t = ff_mul(FF{P.Kh, P.Kl}, d);
+    float tot = ((t.h - rintf(t.h)) + t.l) + (sr.b.z + psi);
+    tot -= rintf(tot);
+    o.ang = tot * kTwoPiF;
+    const FF qq = ff_mul(ff_add(d, FF{-P.rsh, -P.rsl}), FF{P.idrh, P.idrl});
+    float fl = floorf(qq.h);
+    float f = (qq.h - fl) + qq.l;
+    if (f < 0.0f) {
+        f += 1.0f;
+        fl -= 1.0f;
+    } else if (f >= 1.0f) {
+        f -= 1.0f;
+        fl += 1.0f;
+    }
+    if (!(fl >= 1.0f && fl <= (float)(P.in.samples - 3))) return false;
+    const int i = (int)fl;
+    const float2 x0 = __ldg(row + i - 1), x1 = __ldg(row + i), x2 = __ldg(row + i + 1), x3 = __ldg(row + i + 2);
+    float4 c01, c23;
+    cubic_coefficients(x0, x1, x2, x3, 1.0f, c01, c23);
+    const float s = f - 0.5f;
+    o.vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+    o.vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+    if (DERIV) {
+        o.dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
+        o.dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
+        const float inv = 1.0f / d.h;
+        o.ex = (vx.h + vx.l) * inv;
+        o.ey = (vy.h + vy.l) * inv;
+        o.ez = (vz.h + vz.l) * inv;
+        o.d = d.h;
+    }
+    return true;
+}
+
 
 // Per (tile, pulse) record in FP64, computed by lane `lane` of warp 0.  Returns
 // the number of window entries the pulse needs (cap + 1 if it cannot be staged).
+// Two-float record of a pulse the fast path cannot stage (out of line: it is rare, and its
+// FP64 temporaries would otherwise add to the registers of every chunk kernel).
+__device__ __noinline__ void slow_record(const SplitParams& P, const TileShared& S, int n, SlowRec* out) {
+    const PulseInputs& in = P.in;
+    SlowRec sr;
+    split2(S.cx - in.pos[3 * n], sr.a.x, sr.a.y);
+    split2(S.cy - in.pos[3 * n + 1], sr.a.z, sr.a.w);
+    split2(S.cz - in.pos[3 * n + 2], sr.b.x, sr.b.y);
+    const double ph = in.phase[n] * kInvTwoPi;
+    sr.b.z = (float)(ph - rint(ph));
+    sr.b.w = (float)in.weight[n];
+    *out = sr;
+}
+
 __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, Rec* rec, int lane, int n) {
     const PulseInputs& in = P.in;
     const double vx = S.cx - in.pos[3 * n], vy = S.cy - in.pos[3 * n + 1], vz = S.cz - in.pos[3 * n + 2];
@@ -585,18 +679,42 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
     return count;
 }
 
+__device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* srec, int n, int c0, float dxh,
+                                          float dxl, float dyh, float dyl, float dzh, float dzl, float psi) {
+    Pix q;
+    q.dxh = dxh;
+    q.dxl = dxl;
+    q.dyh = dyh;
+    q.dyl = dyl;
+    q.dzh = dzh;
+    q.dzl = dzl;
+    float ar = 0.0f, ai = 0.0f;
+    for (int j = 0; j < n; ++j) {
+        const SlowRec sr = srec[j];
+        SlowSample o;
+        if (!slow_sample<false>(P, sr, P.in.data + (size_t)(c0 + j) * P.in.samples, q, psi, o)) continue;
+        float sn, cs;
+        __sincosf(o.ang, &sn, &cs);
+        const float a = sr.b.w;
+        ar = fmaf(a * o.vr, cs, fmaf(-a * o.vi, sn, ar));
+        ai = fmaf(a * o.vr, sn, fmaf(a * o.vi, cs, ai));
+    }
+    return make_float2(ar, ai);
+}
+
 // Chunk driver shared by the forward and adjoint kernels: per chunk of up to 64
 // pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, FP64,
 // on two SM sub-partitions at once) and pack the pulses' range windows, all warps
 // stage the windows (Horner coefficients, times the pulse weight when `weighted`),
 // then `body.fast(rec, win, nfit, c0)` consumes them; a pulse whose window cannot be
-// staged goes through `body.slow(c0)`.
+// staged goes through `body.slow(c0, n, slow)` with its two-float record.
 template <class Body>
 __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, char* smem, bool weighted, Body& body) {
     const PulseInputs& in = P.in;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Rec* rec = reinterpret_cast<Rec*>(smem);
-    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxChunk * sizeof(Rec));
+    float4* win = reinterpret_cast<float4*>(smem + window_offset());
+    SlowRec* slow = reinterpret_cast<SlowRec*>(win);  // a chunk that stages nothing reuses the window space
     for (int c0 = J.p0; c0 < J.p1;) {
         const int want = min(P.chunk, J.p1 - c0);
         __syncthreads();  // the previous chunk's records and windows are consumed
@@ -640,8 +758,22 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
             body.fast(rec, win, nfit, c0);
             c0 += nfit;
         } else {
-            body.slow(c0);
-            c0 += 1;
+            // The leading pulses that cannot be staged (outside the precision envelope or with
+            // windows too wide): two-float geometry per pixel, [c0, c0 + nslow).
+            // (the records mark them with a window count of cap + 1)
+            if (warp < 2) {
+                const int idx = 32 * warp + lane;
+                const unsigned misses =
+                    __ballot_sync(0xffffffffu, idx < want && __float_as_int(rec[idx].c.w) + 1 > P.cap);
+                if (lane == 0) S.miss_w[warp] = misses;
+            }
+            __syncthreads();
+            const unsigned long long m = (unsigned long long)S.miss_w[0] | ((unsigned long long)S.miss_w[1] << 32);
+            const int nslow = ~m == 0ull ? kMaxChunk : __ffsll((long long)~m) - 1;
+            if (threadIdx.x < nslow) slow_record(P, S, c0 + threadIdx.x, slow + threadIdx.x);
+            __syncthreads();
+            body.slow(c0, nslow, slow);
+            c0 += nslow;
         }
     }
 }
@@ -652,16 +784,14 @@ struct ForwardBody {
     const TileShared& S;
     Pix* px;
     __device__ void fast(const Rec* rec, const float4* win, int nfit, int) { fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px); }
-    __device__ void slow(int c0) {
-        const PulseInputs& in = P.in;
+    __device__ void slow(int c0, int nslow, const SlowRec* srec) {
 #pragma unroll
         for (int k = 0; k < kPX; ++k) {
-            Pix& q = px[k];
-            const float2 v = slow_pixel(in.data, in.samples, in.pos, in.weight, in.phase, in.range_start, P.inv_dr, P.K,
-                                        S.cx + ((double)q.dxh + (double)q.dxl), S.cy + ((double)q.dyh + (double)q.dyl),
-                                        S.cz + ((double)q.dzh + (double)q.dzl), DEMOD ? q.psi : 0.0f, c0, 1);
-            q.ar += v.x;
-            q.ai += v.y;
+            const Pix& q = px[k];
+            const float2 v = slow_pixel(P, srec, nslow, c0, q.dxh, q.dxl, q.dyh, q.dyl, q.dzh, q.dzl,
+                                        DEMOD ? q.psi : 0.0f);
+            px[k].ar += v.x;
+            px[k].ai += v.y;
         }
     }
 };
@@ -776,60 +906,44 @@ struct AdjointBody {
         flush(c0, nfit);
     }
 
-    // A pulse whose window does not fit: per-sample FP64 geometry, FP32 interpolation.
-    __device__ void slow(int c0) {
+    // Pulses the fast path cannot stage: two-float geometry per pixel, FP32 interpolation.
+    __device__ void slow(int c0, int nslow, const SlowRec* srec) {
         const PulseInputs& in = P.in;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        const int n = c0;
-        const double pxn = in.pos[3 * n], pyn = in.pos[3 * n + 1], pzn = in.pos[3 * n + 2];
-        const double ph = in.phase[n] * kInvTwoPi;
-        const float2* row = in.data + (size_t)n * in.samples;
         const float kr = P.Kf * kTwoPiF, inv_dr = P.inv_drf;
-        float v5[kAdjVals] = {0.f, 0.f, 0.f, 0.f, 0.f};
-        for (int k = 0; k < kPX; ++k) {
-            const Pix& q = px[k];
-            const double x = S.cx + ((double)q.dxh + (double)q.dxl) - pxn;
-            const double y = S.cy + ((double)q.dyh + (double)q.dyl) - pyn;
-            const double z = S.cz + ((double)q.dzh + (double)q.dzl) - pzn;
-            const double d = sqrt(x * x + y * y + z * z);
-            const double t = P.K * d + ph;
-            const float tot = (float)(t - rint(t)) + (DEMOD ? q.psi : 0.0f);
-            const float ang = (tot - round_magic(tot)) * kTwoPiF;
-            const double qq = (d - in.range_start) * P.inv_dr;
-            const double fl = floor(qq);
-            if (!(fl >= 1.0 && fl <= (double)(in.samples - 3))) continue;
-            const int i = (int)fl;
-            const float2 x0 = __ldg(row + i - 1), x1 = __ldg(row + i), x2 = __ldg(row + i + 1), x3 = __ldg(row + i + 2);
-            float4 c01, c23;
-            cubic_coefficients(x0, x1, x2, x3, 1.0f, c01, c23);
-            const float s = (float)(qq - fl - 0.5);
-            const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
-            const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
-            const float dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
-            const float dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
-            float sn, cs;
-            __sincosf(ang, &sn, &cs);
-            const float gr = gre[k], gi = gim[k];
-            const float er = vr * cs - vi * sn, ei = vr * sn + vi * cs;
-            v5[0] = fmaf(gr, er, fmaf(gi, ei, v5[0]));
-            v5[1] = fmaf(gr, ei, fmaf(-gi, er, v5[1]));
-            const float zr = fmaf(dvr, inv_dr, -kr * vi), zi = fmaf(dvi, inv_dr, kr * vr);
-            const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
-            const float tt = fmaf(gr, fr, gi * fi) / (float)d;
-            v5[2] = fmaf(tt, (float)x, v5[2]);
-            v5[3] = fmaf(tt, (float)y, v5[3]);
-            v5[4] = fmaf(tt, (float)z, v5[4]);
-        }
+#pragma unroll 1
+        for (int j = 0; j < nslow; ++j) {
+            const SlowRec sr = srec[j];
+            const float2* row = in.data + (size_t)(c0 + j) * in.samples;
+            float v5[kAdjVals] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int v = 0; v < kAdjVals; ++v) {
+            for (int k = 0; k < kPX; ++k) {
+                SlowSample o;
+                if (!slow_sample<true>(P, sr, row, px[k], DEMOD ? px[k].psi : 0.0f, o)) continue;
+                float sn, cs;
+                __sincosf(o.ang, &sn, &cs);
+                const float gr = gre[k], gi = gim[k];
+                const float er = o.vr * cs - o.vi * sn, ei = o.vr * sn + o.vi * cs;
+                v5[0] = fmaf(gr, er, fmaf(gi, ei, v5[0]));
+                v5[1] = fmaf(gr, ei, fmaf(-gi, er, v5[1]));
+                const float zr = fmaf(o.dvr, inv_dr, -kr * o.vi), zi = fmaf(o.dvi, inv_dr, kr * o.vr);
+                const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
+                const float t = fmaf(gr, fr, gi * fi);
+                v5[2] = fmaf(t, o.ex, v5[2]);
+                v5[3] = fmaf(t, o.ey, v5[3]);
+                v5[4] = fmaf(t, o.ez, v5[4]);
+            }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v5[v] += __shfl_xor_sync(0xffffffffu, v5[v], o);
-        }
-        if (lane == 0) {
+            for (int v = 0; v < kAdjVals; ++v) {
 #pragma unroll
-            for (int v = 0; v < kAdjVals; ++v) red[warp][0][v] = v5[v];
+                for (int o = 16; o > 0; o >>= 1) v5[v] += __shfl_xor_sync(0xffffffffu, v5[v], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int v = 0; v < kAdjVals; ++v) red[warp][j][v] = v5[v];
+            }
         }
-        flush(c0, 1);
+        flush(c0, nslow);
     }
 };
 
@@ -868,7 +982,7 @@ __global__ void __launch_bounds__(kThreads, 3) split_polar_kernel(SplitParams P,
     tile_of(blockIdx.x, g.win_nu, J.lc, J.tile_r, J.tile_u);
     split_range(g.a, g.b, P.pulse_split, blockIdx.y, J.p0, J.p1);
     Pix px[kPX];
-    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + (size_t)kMaxChunk * sizeof(Rec));
+    PolarTables& T = *reinterpret_cast<PolarTables*>(smem + window_offset());
     setup_polar(P, J, S, T, px, true);
     pulse_loop<false, true>(P, J, S, smem, px);
     store_window(J, g.win_nr, g.win_nu, px, P.out + blockIdx.y * P.split_stride, P.out_stride);
@@ -1475,10 +1589,16 @@ SplitParams make_params(const PulseInputs& in, int chunk, int cap, int pulse_spl
     P.Kf = (float)P.K;
     P.inv_drf = (float)P.inv_dr;
     P.chunk = chunk < 1 ? 1 : (chunk > kMaxChunk ? kMaxChunk : chunk);
-    P.cap = cap < 4 ? 4 : cap;
+    P.cap = cap < 64 ? 64 : cap;  // >= kMaxChunk two-float records (32 bytes each) fit the window space
     P.pulse_split = pulse_split;
     P.split_stride = 0;
     P.envelope = kDirectEnvelope;
+    P.Kh = (float)P.K;
+    P.Kl = (float)(P.K - (double)P.Kh);
+    P.rsh = (float)in.range_start;
+    P.rsl = (float)(in.range_start - (double)P.rsh);
+    P.idrh = (float)P.inv_dr;
+    P.idrl = (float)(P.inv_dr - (double)P.idrh);
     return P;
 }
 
@@ -1487,7 +1607,7 @@ size_t merge_smem() { return sizeof(TabF); }
 size_t dynamic_smem(int cap, bool polar) {
     size_t win = (size_t)cap * 32;
     if (polar && win < sizeof(PolarTables)) win = sizeof(PolarTables);
-    return (size_t)kMaxChunk * sizeof(Rec) + win;
+    return window_offset() + win;
 }
 
 template <class K>
@@ -1861,8 +1981,7 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     b.has_z = (d.lat.step_row[2] != 0.0 || d.lat.step_col[2] != 0.0) ? 1 : 0;
     b.prec_offset = d.prec_offset;
     memcpy(dst, &b, sizeof(b));
-    return (d.kind == 0 ? (size_t)kMaxChunk * sizeof(Rec) : (size_t)kMaxLeafChunk * sizeof(LeafRec)) +
-           (size_t)b.P.cap * 32;
+    return (d.kind == 0 ? window_offset() : (size_t)kMaxLeafChunk * sizeof(LeafRec)) + (size_t)b.P.cap * 32;
 }
 
 int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_sm, int* leaf_per_sm,

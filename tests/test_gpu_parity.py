@@ -202,6 +202,29 @@ def test_ragged_and_edge_lattices_vs_fp64_oracle(lib, shape, step, tilt, shift):
         assert err <= tol
 
 
+def test_points_outside_the_envelope_match_fp64(lib):
+    """Points scattered over the whole scene: every 1024-point tile is too wide for the split
+    path's precision envelope, so every pulse takes the two-float fallback; it must still meet
+    the split tolerance against the FP64 oracle (and the tiles that fit still use the fast path)."""
+    from bp_project_gb300 import core
+    from oracle import reference as ora
+    sc = _scene("c0", pulses=384, image_side=256)
+    rng = np.random.default_rng(12)
+    lat = sc.lattice
+    span = lat.rows * lat.step_row[0]
+    pts = np.column_stack([lat.origin[0] + rng.uniform(0, span, 3000), lat.origin[1] + rng.uniform(0, span, 3000),
+                           rng.uniform(-2, 2, 3000)])
+    _, ref = ora.backproject_points(sc.data, sc.position, pts, sc.range_start, sc.data_dr, sc.k, sc.weight, sc.phase,
+                                    c128=True)
+    args = [_dev(a, dt) for a, dt in ((sc.data, torch.complex64), (sc.position, torch.float64),
+                                      (sc.weight, torch.float64), (sc.phase, torch.float64))]
+    out = core.backproject_points(*args, _dev(pts, torch.float64), sc.range_start, sc.data_dr, sc.k,
+                                  mode="split").cpu().numpy()
+    err = rel_err(ref, out)
+    print(f"scattered points (two-float fallback): {err:.2e}")
+    assert err <= 1e-5
+
+
 def test_evaluate_lattice_matches_points_path(lib):
     """Split-precision evaluate onto the 512^2 ground lattice vs the FP64-geometry points kernel."""
     from bp_project_gb300 import core
