@@ -62,6 +62,8 @@ struct Pix {
 
 struct TileShared {
     double cx, cy, cz;
+    float ch[3], cl[3];         // the centre as two-float (hi + lo), for the FP32 records
+    float rhof;
     double rho;                 // bound on |delta_p| (m)
     double scale_d, inv_scale_d;
     double sum[4];
@@ -643,34 +645,65 @@ __device__ __noinline__ void slow_record(const SplitParams& P, const TileShared&
     *out = sr;
 }
 
+// Per (tile, pulse) record, computed by lane `lane` of the record warps in two-float FP32
+// arithmetic (about 44 bits; GB300's FP64 rate would make these records the barrier-bound
+// part of every chunk).  Returns the number of window entries the pulse needs (cap + 1 if
+// it cannot be staged).
 __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, Rec* rec, int lane, int n) {
     const PulseInputs& in = P.in;
-    const double vx = S.cx - in.pos[3 * n], vy = S.cy - in.pos[3 * n + 1], vz = S.cz - in.pos[3 * n + 2];
-    const double R = sqrt(vx * vx + vy * vy + vz * vz);
-    const double iR = 1.0 / R;
-    const double ux = vx * iR, uy = vy * iR, uz = vz * iR;
-    const double t1 = P.K * R + in.phase[n] * kInvTwoPi;
-    const double Q = (R - in.range_start) * P.inv_dr;
-    const double I = floor(Q);
-    const double Fm = (Q - I) - 0.5;
+    float ph_, pl_;
+    split2(in.pos[3 * n], ph_, pl_);
+    const FF vx = ff_add(FF{S.ch[0], S.cl[0]}, FF{-ph_, -pl_});
+    split2(in.pos[3 * n + 1], ph_, pl_);
+    const FF vy = ff_add(FF{S.ch[1], S.cl[1]}, FF{-ph_, -pl_});
+    split2(in.pos[3 * n + 2], ph_, pl_);
+    const FF vz = ff_add(FF{S.ch[2], S.cl[2]}, FF{-ph_, -pl_});
+    const FF R = ff_sqrt(ff_add(ff_add(ff_sqr(vx), ff_sqr(vy)), ff_sqr(vz)));
+    // 1/R: the FP32 reciprocal refined by one Newton step in two-float.
+    const float i0 = __frcp_rn(R.h);
+    const FF e = ff_mul(R, FF{i0, 0.0f});
+    const FF iR = ff_norm(i0, i0 * ((1.0f - e.h) - e.l));
+    const FF ux = ff_mul(vx, iR), uy = ff_mul(vy, iR), uz = ff_mul(vz, iR);
+    const FF Kk{P.Kh, P.Kl};
+    const FF t = ff_mul(Kk, R);
+    const double ph = in.phase[n] * kInvTwoPi;
+    float t1 = ((t.h - rintf(t.h)) + t.l) + (float)(ph - rint(ph));
+    t1 -= rintf(t1);
+    const FF Q = ff_mul(ff_add(R, FF{-P.rsh, -P.rsl}), FF{P.idrh, P.idrl});
+    float I = floorf(Q.h);
+    float fq = (Q.h - I) + Q.l;
+    if (fq < 0.0f) {
+        fq += 1.0f;
+        I -= 1.0f;
+    } else if (fq >= 1.0f) {
+        fq -= 1.0f;
+        I += 1.0f;
+    }
+    const float Fm = fq - 0.5f;
+    const float Rf = R.h, uxf = ux.h + ux.l, uyf = uy.h + uy.l, uzf = uz.h + uz.l;
     // |L| <= sum_c |u_c| bound_c and 0 <= eps <= rho^2 / (2 (R - rho)), in bins.
-    const double lin = fabs(ux) * S.bnd[0] + fabs(uy) * S.bnd[1] + fabs(uz) * S.bnd[2];
-    const double eps = S.rho * S.rho / (2.0 * fmax(R - S.rho, 1.0));
-    const double hw = (lin + eps) * fabs(P.inv_dr) + 1e-3;
-    const double lo = floor(Fm - hw), hi = ceil(Fm + hw);
-    const bool ok = R > 0.0 && fabs(Q) < 1.0e9 && hi - lo + 1.0 <= (double)P.cap &&
-                    fabs(P.K) * S.rho * S.rho <= P.envelope * R && S.rho < 0.25 * R;
+    const float lin = fabsf(uxf) * S.bnd[0] + fabsf(uyf) * S.bnd[1] + fabsf(uzf) * S.bnd[2];
+    const float eps = S.rhof * S.rhof / (2.0f * fmaxf(Rf - S.rhof, 1.0f));
+    const float hw = (lin + eps) * fabsf(P.inv_drf) + 1e-3f;
+    const float lo = floorf(Fm - hw), hi = ceilf(Fm + hw);
+    const bool ok = Rf > 0.0f && fabsf(Q.h) < 1.0e7f && hi - lo + 1.0f <= (float)P.cap &&
+                    fabsf(P.Kf) * S.rhof * S.rhof <= (float)P.envelope * Rf && S.rhof < 0.25f * Rf;
     const int bo = ok ? (int)lo : 0;
     S.base[lane] = ok ? (int)I + bo : 0;
     S.wt[lane] = (float)in.weight[n];
+    const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
     Rec r;
-    quantize(P.K * ux, P.scale_w, P.inv_scale_w, r.a.x, r.a.z);
-    quantize(P.K * uy, P.scale_w, P.inv_scale_w, r.a.y, r.a.w);
-    quantize(P.K * uz, P.scale_w, P.inv_scale_w, r.d.y, r.d.z);
-    r.b = make_float4((float)ux, (float)uy, (float)(2.0 * R), (float)Fm);
-    r.c.x = (float)(t1 - rint(t1));
+    const FF Wx = ff_mul(Kk, ux), Wy = ff_mul(Kk, uy), Wz = ff_mul(Kk, uz);
+    r.a.x = rintf(Wx.h * isw) * sw;
+    r.a.z = (Wx.h - r.a.x) + Wx.l;
+    r.a.y = rintf(Wy.h * isw) * sw;
+    r.a.w = (Wy.h - r.a.y) + Wy.l;
+    r.d.y = rintf(Wz.h * isw) * sw;
+    r.d.z = (Wz.h - r.d.y) + Wz.l;
+    r.b = make_float4(uxf, uyf, 2.0f * Rf, Fm);
+    r.c.x = t1;
     r.c.y = __int_as_float(kMagicBits + bo);
-    r.d.x = (float)uz;
+    r.d.x = uzf;
     r.d.w = 0.0f;
     const int count = ok ? (int)(hi - lo) + 1 : P.cap + 1;
     r.c.z = 0.0f;
@@ -715,6 +748,12 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
     Rec* rec = reinterpret_cast<Rec*>(smem);
     float4* win = reinterpret_cast<float4*>(smem + window_offset());
     SlowRec* slow = reinterpret_cast<SlowRec*>(win);  // a chunk that stages nothing reuses the window space
+    if (threadIdx.x == 0) {  // the tile centre as two-float for the records (ordered by the loop's barrier)
+        split2(S.cx, S.ch[0], S.cl[0]);
+        split2(S.cy, S.ch[1], S.cl[1]);
+        split2(S.cz, S.ch[2], S.cl[2]);
+        S.rhof = (float)S.rho;
+    }
     for (int c0 = J.p0; c0 < J.p1;) {
         const int want = min(P.chunk, J.p1 - c0);
         __syncthreads();  // the previous chunk's records and windows are consumed
