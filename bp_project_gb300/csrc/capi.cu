@@ -90,6 +90,7 @@ PolarDesc desc_of(const sarbp_polar_grid& g) {
     d.out_offset = 0;
     d.out_stride = g.nu;
     d.tile_lc = 5;
+    split_geometry(d);
     return d;
 }
 
@@ -605,7 +606,7 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
         if (st == SARBP_OK)
             st = launch_split_ffbp_leaf_pulses(in, nodes, leaves, (int)plan->leaves.size(), precs, s);
         if (st == SARBP_OK)
-            st = launch_split_ffbp_child_records(k, nodes, items + plan->stage_begin[0] + plan->stage_count[0],
+            st = launch_split_ffbp_child_records(k, nodes, tables, items + plan->stage_begin[0] + plan->stage_count[0],
                                                  (int)plan->merge_items, arena, crecs, s);
         if (st == SARBP_OK)
             st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb,

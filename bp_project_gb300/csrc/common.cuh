@@ -96,7 +96,19 @@ struct PolarDesc {
     long long rows_off;                  // FFBP: first entry of this node's row table (float4 (g_hi, g_lo, psi, 0))
     long long cols_off;                  // FFBP: first entry of this node's column table (float4 (c_hi, c_lo, u_hi, u_lo))
     float2* dst;                         // if set: where the node's window is written (batched scene roots)
+    // The FP64 geometry as two-float pairs (hi, lo), split on the host, so that per-tile set-up
+    // on the GPU needs no FP64: origin x/y/z, r0, dr, u0, du, 1/dr, 1/du.
+    float2 tf[9];
 };
+
+// Fills PolarDesc::tf from the FP64 fields (host).
+inline void split_geometry(PolarDesc& d) {
+    const double v[9] = {d.ox, d.oy, d.oz, d.r0, d.dr, d.u0, d.du, 1.0 / d.dr, 1.0 / d.du};
+    for (int i = 0; i < 9; ++i) {
+        const float h = (float)v[i];
+        d.tf[i] = make_float2(h, (float)(v[i] - (double)h));
+    }
+}
 
 struct TileItem {
     int node;
@@ -221,8 +233,8 @@ int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int 
                              float4* tables, cudaStream_t s);
 int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes, const int* leaves, int n_leaves,
                                   void* recs, cudaStream_t s);
-int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const TileItem* items, int n_items,
-                                    float2* arena, void* recs, cudaStream_t s);
+int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const float4* tables, const TileItem* items,
+                                    int n_items, float2* arena, void* recs, cudaStream_t s);
 size_t split_ffbp_pulse_record_bytes();
 size_t split_ffbp_child_record_bytes();
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,

@@ -555,6 +555,29 @@ __device__ __forceinline__ FF ff_sqrt(FF a) {
     const float r = ((a.h - p) - e) + a.l;
     return ff_norm(s, r * (0.5f / s));
 }
+__device__ __forceinline__ FF ff_of(float2 v) { return FF{v.x, v.y}; }
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.h, -a.l}; }
+// 1/a: the FP32 reciprocal refined by one Newton step in two-float.
+__device__ __forceinline__ FF ff_rcp(FF a) {
+    const float i0 = __frcp_rn(a.h);
+    const FF e = ff_mul(a, FF{i0, 0.0f});
+    return ff_norm(i0, i0 * ((1.0f - e.h) - e.l));
+}
+// Splits a two-float value q into floor and centred fraction: q = I + F + 1/2, F in [-1/2, 1/2).
+__device__ __forceinline__ float ff_floor_frac(FF q, float& F) {
+    float I = floorf(q.h);
+    float f = (q.h - I) + q.l;  // q.h - I is exact
+    if (f < 0.0f) {
+        f += 1.0f;
+        I -= 1.0f;
+    } else if (f >= 1.0f) {
+        f -= 1.0f;
+        I += 1.0f;
+    }
+    F = f - 0.5f;
+    return I;
+}
+
 
 // Per (tile, pulse) data of a pulse the fast path cannot stage: the FP64 vector from the
 // antenna to the tile centre as two-float components, the pulse phase in turns, the weight.
@@ -1150,33 +1173,48 @@ __global__ void __launch_bounds__(kThreads) adjoint_sum_kernel(const float* __re
 }
 
 // ---- FFBP: per-node tables and per-pulse leaf records (prologue kernels) ------------------
-__device__ __forceinline__ void table_entries(double K, double range_start, double inv_dr, const PolarDesc& g, int t,
+// Two-float constants of the table entries: K (turns/m), range_start, 1 / data_dr.
+struct TableConsts {
+    float Kh, Kl, rsh, rsl, idrh, idrl;
+};
+
+__host__ __device__ inline TableConsts table_consts(const SplitParams& P) {
+    return TableConsts{P.Kh, P.Kl, P.rsh, P.rsl, P.idrh, P.idrl};
+}
+
+__device__ __forceinline__ FF ff_sqrt0(FF a) { return a.h > 0.0f ? ff_sqrt(a) : FF{0.0f, 0.0f}; }
+
+// Row t and column t of node g's tables in two-float FP32 arithmetic from the node geometry
+// split on the host (PolarDesc::tf).
+__device__ __forceinline__ void table_entries(const TableConsts& C, const PolarDesc& g, int t,
                                               float4* __restrict__ tables) {
+    const FF ft{(float)t, 0.0f};  // exact: node dimensions are far below 2^24
     if (t < g.nr) {
-        const double r = g.r0 + (double)t * g.dr;
-        const double gg = sqrt(fmax(0.0, r * r - g.oz * g.oz));
-        const float gh = (float)gg;
-        const double ph = -K * r;
-        const double gr = gg / r, ez = -g.oz / r;
-        const float grh = (float)gr, ezh = (float)ez;
-        const double Q = (r - range_start) * inv_dr;
-        const double I = fmin(fmax(floor(Q), -1.0e9), 1.0e9);
+        const FF r = ff_add(ff_of(g.tf[3]), ff_mul(ft, ff_of(g.tf[4])));
+        const FF oz = ff_of(g.tf[2]);
+        const FF gg = ff_sqrt0(ff_add(ff_sqr(r), ff_neg(ff_sqr(oz))));
+        const FF ph = ff_mul(FF{-C.Kh, -C.Kl}, r);
+        float psi = (ph.h - rintf(ph.h)) + ph.l;
+        psi -= rintf(psi);
+        const FF ir = ff_rcp(r);
+        const FF gr = ff_mul(gg, ir), ez = ff_mul(ff_neg(oz), ir);
+        float F;
+        const float I = fminf(fmaxf(ff_floor_frac(ff_mul(ff_add(r, FF{-C.rsh, -C.rsl}), FF{C.idrh, C.idrl}), F),
+                                    -1.0e9f), 1.0e9f);
         float4* row = tables + g.rows_off + 3 * (long long)t;
-        row[0] = make_float4(gh, (float)(gg - (double)gh), (float)(ph - rint(ph)), 0.0f);
-        row[1] = make_float4(grh, (float)(gr - (double)grh), ezh, (float)(ez - (double)ezh));
-        row[2] = make_float4((float)(2.0 * r), (float)(Q - I - 0.5), __int_as_float((int)I), 0.0f);
+        row[0] = make_float4(gg.h, gg.l, psi, 0.0f);
+        row[1] = make_float4(gr.h, gr.l, ez.h, ez.l);
+        row[2] = make_float4(2.0f * (r.h + r.l), F, __int_as_float((int)I), 0.0f);
     }
     if (t < g.nu) {
-        const double u = g.u0 + (double)t * g.du;
-        const double c = sqrt(fmax(0.0, 1.0 - u * u));
-        const float chh = (float)c, uh = (float)u;
-        tables[g.cols_off + t] = make_float4(chh, (float)(c - (double)chh), uh, (float)(u - (double)uh));
+        const FF u = ff_add(ff_of(g.tf[5]), ff_mul(ft, ff_of(g.tf[6])));
+        const FF c = ff_sqrt0(ff_add(FF{1.0f, 0.0f}, ff_neg(ff_sqr(u))));
+        tables[g.cols_off + t] = make_float4(c.h, c.l, u.h, u.l);
     }
 }
 
-__global__ void ffbp_tables_kernel(double K, double range_start, double inv_dr, const PolarDesc* __restrict__ nodes,
-                                   float4* __restrict__ tables) {
-    table_entries(K, range_start, inv_dr, nodes[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x, tables);
+__global__ void ffbp_tables_kernel(TableConsts C, const PolarDesc* __restrict__ nodes, float4* __restrict__ tables) {
+    table_entries(C, nodes[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x, tables);
 }
 
 // Leaf pulses relative to the leaf's phase centre O (origin formulation).
@@ -1442,32 +1480,40 @@ struct ChildRec {
     const float2* img;
 };
 
-// One thread per (merge tile, child): the tile centre is the FP64 position of
-// the tile's centre pixel, the same point setup_polar_tab measures offsets from.
-// FP64 record of a polar image c seen from the ground point (px, py, 0): the FP32
-// quantities child_value needs for points near it (a parent tile, or a lattice tile).
-__device__ __forceinline__ ChildRec child_rec_at(double K, double scale_w, double inv_scale_w, const PolarDesc& c,
-                                                 double px, double py, const float2* img) {
-    const double vx = px - c.ox, vy = py - c.oy, vz = -c.oz;
-    const double g2 = vx * vx + vy * vy;
-    const double G = sqrt(g2);
-    const double RR = sqrt(g2 + vz * vz);
-    const double ux = vx / RR, uy = vy / RR;
-    const double t1 = K * RR;
-    const double qr = (RR - c.r0) / c.dr;
-    const double ir = floor(qr);
-    const double hx = vx / G, hy = vy / G;
-    const double qu = (hy - c.u0) / c.du;
-    const double iu = floor(qu);
+// Record of a polar image c seen from the ground point (px, py, 0), in two-float FP32
+// arithmetic from the node geometry split on the host (PolarDesc::tf): the FP32 quantities
+// child_value needs for points near it (a parent tile, or a lattice tile).  K in turns/m.
+__device__ __forceinline__ ChildRec child_rec_at(FF K, float scale_w, float inv_scale_w, const PolarDesc& c, FF px,
+                                                 FF py, const float2* img) {
+    const FF vx = ff_add(px, ff_neg(ff_of(c.tf[0])));
+    const FF vy = ff_add(py, ff_neg(ff_of(c.tf[1])));
+    const FF vz = ff_neg(ff_of(c.tf[2]));
+    const FF g2 = ff_add(ff_sqr(vx), ff_sqr(vy));
+    const FF G = ff_sqrt(g2);
+    const FF RR = ff_sqrt(ff_add(g2, ff_sqr(vz)));
+    const FF iR = ff_rcp(RR), iG = ff_rcp(G);
+    const FF ux = ff_mul(vx, iR), uy = ff_mul(vy, iR);
+    const FF hy = ff_mul(vy, iG);
+    const FF t = ff_mul(K, RR);
+    float phi = (t.h - rintf(t.h)) + t.l;
+    phi -= rintf(phi);
+    float fr, fu;
+    const FF Qr = ff_mul(ff_add(RR, ff_neg(ff_of(c.tf[3]))), ff_of(c.tf[7]));
+    const FF Qu = ff_mul(ff_add(hy, ff_neg(ff_of(c.tf[5]))), ff_of(c.tf[8]));
+    const float ir = ff_floor_frac(Qr, fr), iu = ff_floor_frac(Qu, fu);
+    const FF Wx = ff_mul(K, ux), Wy = ff_mul(K, uy);
     ChildRec R;
-    quantize(K * ux, scale_w, inv_scale_w, R.a.x, R.a.z);
-    quantize(K * uy, scale_w, inv_scale_w, R.a.y, R.a.w);
-    R.b = make_float4((float)ux, (float)uy, (float)(2.0 * RR), (float)(qr - ir - 0.5));
-    R.c = make_float4((float)(t1 - rint(t1)), (float)hx, (float)hy, (float)(2.0 * G));
-    R.d = make_float4((float)G, (float)(qu - iu - 0.5), 0.0f, 0.0f);
-    R.inv_sdr = (float)(1.0 / c.dr);
-    R.inv_sdu = (float)(1.0 / c.du);
-    const bool ok = fabs(ir) < 1.0e9 && fabs(iu) < 1.0e9 && G > 0.0;
+    R.a.x = rintf(Wx.h * inv_scale_w) * scale_w;  // scale_w is a power of two: exact
+    R.a.z = (Wx.h - R.a.x) + Wx.l;
+    R.a.y = rintf(Wy.h * inv_scale_w) * scale_w;
+    R.a.w = (Wy.h - R.a.y) + Wy.l;
+    const float Gf = G.h + G.l;
+    R.b = make_float4(ux.h + ux.l, uy.h + uy.l, 2.0f * (RR.h + RR.l), fr);
+    R.c = make_float4(phi, ff_mul(vx, iG).h, hy.h + hy.l, 2.0f * Gf);
+    R.d = make_float4(Gf, fu, 0.0f, 0.0f);
+    R.inv_sdr = c.tf[7].x;
+    R.inv_sdu = c.tf[8].x;
+    const bool ok = fabsf(Qr.h) < 1.0e7f && fabsf(Qu.h) < 1.0e7f && G.h > 0.0f;  // false for NaN
     R.ir0 = ok ? (int)ir : -(1 << 30);
     R.iu0 = ok ? (int)iu : -(1 << 30);
     R.snr = c.nr;
@@ -1476,28 +1522,34 @@ __device__ __forceinline__ ChildRec child_rec_at(double K, double scale_w, doubl
     return R;
 }
 
-__device__ __forceinline__ void child_record(double K, double scale_w, double inv_scale_w,
-                                             const PolarDesc* __restrict__ nodes, const TileItem it, int t,
-                                             float2* __restrict__ arena, ChildRec* __restrict__ out) {
+// One thread per (merge tile, child).  The tile centre is the centre pixel's position from
+// the node's row and column tables (two-float g and c, u), the same point setup_polar_tab
+// measures the pixel offsets from.
+__device__ __forceinline__ void child_record(FF K, float scale_w, float inv_scale_w,
+                                             const PolarDesc* __restrict__ nodes, const float4* __restrict__ tables,
+                                             const TileItem it, int t, float2* __restrict__ arena,
+                                             ChildRec* __restrict__ out) {
     const PolarDesc& g = nodes[it.node];
     const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
     const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
     const int i0 = min(g.win_r0 + it.tile_r + (rows_t >> 1), g.nr - 1);
     const int j0 = min(g.win_u0 + it.tile_u + (cols_t >> 1), g.nu - 1);
-    const double rc = g.r0 + (double)i0 * g.dr;
-    const double g0 = sqrt(fmax(0.0, rc * rc - g.oz * g.oz));
-    const double uc = g.u0 + (double)j0 * g.du;
-    const double c0 = sqrt(fmax(0.0, 1.0 - uc * uc));
-    out[t] = child_rec_at(K, scale_w, inv_scale_w, c, g.ox + (double)g.side * g0 * c0, g.oy + g0 * uc,
-                          arena + c.out_offset);
+    const float4 rv = __ldg(tables + g.rows_off + 3 * (long long)i0);
+    const float4 cv = __ldg(tables + g.cols_off + j0);
+    const FF g0{rv.x, rv.y};
+    const FF gc = ff_mul(g0, FF{cv.x, cv.y});
+    const FF px = ff_add(ff_of(g.tf[0]), g.side < 0 ? ff_neg(gc) : gc);
+    const FF py = ff_add(ff_of(g.tf[1]), ff_mul(g0, FF{cv.z, cv.w}));
+    out[t] = child_rec_at(K, scale_w, inv_scale_w, c, px, py, arena + c.out_offset);
 }
 
-__global__ void ffbp_child_records_kernel(double K, double scale_w, double inv_scale_w,
-                                          const PolarDesc* __restrict__ nodes, const TileItem* __restrict__ items,
-                                          int n_items, float2* __restrict__ arena, ChildRec* __restrict__ out) {
+__global__ void ffbp_child_records_kernel(float Kh, float Kl, float scale_w, float inv_scale_w,
+                                          const PolarDesc* __restrict__ nodes, const float4* __restrict__ tables,
+                                          const TileItem* __restrict__ items, int n_items,
+                                          float2* __restrict__ arena, ChildRec* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * n_items) return;
-    child_record(K, scale_w, inv_scale_w, nodes, items[t >> 1], t, arena, out);
+    child_record(FF{Kh, Kl}, scale_w, inv_scale_w, nodes, tables, items[t >> 1], t, arena, out);
 }
 
 // Child-image coordinates of a parent pixel: bin indices (ir, iu), centred fractions
@@ -1790,7 +1842,7 @@ int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int 
                              float4* tables, cudaStream_t s) {
     if (n_nodes <= 0) return SARBP_OK;
     dim3 grid((max_dim + kThreads - 1) / kThreads, n_nodes);
-    ffbp_tables_kernel<<<grid, kThreads, 0, s>>>(in.k * kInvTwoPi, in.range_start, 1.0 / in.data_dr, nodes, tables);
+    ffbp_tables_kernel<<<grid, kThreads, 0, s>>>(table_consts(make_params(in, 1, 4, 1)), nodes, tables);
     note_launches(1);
     return check_launch("split_ffbp_tables");
 }
@@ -1804,15 +1856,16 @@ int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes,
     return check_launch("split_ffbp_leaf_pulses");
 }
 
-int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const TileItem* items, int n_items,
-                                    float2* arena, void* recs, cudaStream_t s) {
+int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const float4* tables, const TileItem* items,
+                                    int n_items, float2* arena, void* recs, cudaStream_t s) {
     if (n_items <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
     none.data_dr = 1.0;
     const SplitParams P = make_params(none, 1, 4, 1);
     ffbp_child_records_kernel<<<grid_blocks(2LL * n_items, kThreads), kThreads, 0, s>>>(
-        P.K, P.scale_w, P.inv_scale_w, nodes, items, n_items, arena, reinterpret_cast<ChildRec*>(recs));
+        P.Kh, P.Kl, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, items, n_items, arena,
+        reinterpret_cast<ChildRec*>(recs));
     note_launches(1);
     return check_launch("split_ffbp_child_records");
 }
@@ -1852,11 +1905,11 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
 // ---- polar image -> ground lattice (evaluate_image on a lattice, split precision) -----------
 //
 // A lattice tile is a parent tile whose pixels lie on the ground lattice, and the polar
-// image is its only child: one FP64 record per tile (child_rec_at at the tile centre),
+// image is its only child: one two-float record per tile (child_rec_at at the tile centre),
 // then per pixel the merge kernel's FP32 child coordinates, 4x4 stencil and phase.  The
 // phase restores exp(j k r) (r: the point's range to the image origin); no demodulation.
-__global__ void __launch_bounds__(kThreads, 3) split_evaluate_lattice_kernel(double K, double scale_w,
-                                                                             double inv_scale_w, PolarDesc c,
+__global__ void __launch_bounds__(kThreads, 3) split_evaluate_lattice_kernel(float Kh, float Kl, float scale_w,
+                                                                             float inv_scale_w, PolarDesc c,
                                                                              const float2* __restrict__ img,
                                                                              sarbp_lattice lat, int lc,
                                                                              float2* __restrict__ out) {
@@ -1868,9 +1921,14 @@ __global__ void __launch_bounds__(kThreads, 3) split_evaluate_lattice_kernel(dou
     tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
     Pix px[kPX];
     setup_lattice<false>(J, S, px);
-    if (threadIdx.x == 0) C = child_rec_at(K, scale_w, inv_scale_w, c, S.cx, S.cy, img);
+    if (threadIdx.x == 0) {
+        FF x, y;
+        split2(S.cx, x.h, x.l);
+        split2(S.cy, y.h, y.l);
+        C = child_rec_at(FF{Kh, Kl}, scale_w, inv_scale_w, c, x, y, img);
+    }
     __syncthreads();
-    const float Kf = (float)K;
+    const float Kf = Kh;
     const int cols_t = 1 << lc;
 #pragma unroll
     for (int k = 0; k < kPX; ++k) {
@@ -1985,7 +2043,7 @@ __global__ void batch_tables_kernel(const BatchScene* __restrict__ scenes, const
                                     float4* __restrict__ tables) {
     const PolarDesc& g = nodes[blockIdx.y];
     const SplitParams& P = scenes[g.pad].P;
-    table_entries(P.K, P.in.range_start, P.inv_dr, g, blockIdx.x * blockDim.x + threadIdx.x, tables);
+    table_entries(table_consts(P), g, blockIdx.x * blockDim.x + threadIdx.x, tables);
 }
 
 __global__ void batch_leaf_pulses_kernel(const BatchScene* __restrict__ scenes, const PolarDesc* __restrict__ nodes,
@@ -1997,13 +2055,13 @@ __global__ void batch_leaf_pulses_kernel(const BatchScene* __restrict__ scenes, 
 }
 
 __global__ void batch_child_records_kernel(const BatchScene* __restrict__ scenes, const PolarDesc* __restrict__ nodes,
-                                           const TileItem* __restrict__ items, int n_items, float2* __restrict__ arena,
-                                           ChildRec* __restrict__ out) {
+                                           const float4* __restrict__ tables, const TileItem* __restrict__ items,
+                                           int n_items, float2* __restrict__ arena, ChildRec* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * n_items) return;
     const TileItem it = items[t >> 1];
     const SplitParams& P = scenes[it.pad].P;
-    child_record(P.K, P.scale_w, P.inv_scale_w, nodes, it, t, arena, out);
+    child_record(FF{P.Kh, P.Kl}, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, it, t, arena, out);
 }
 
 }  // namespace
@@ -2055,7 +2113,7 @@ int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int 
     }
     if (n_merge_items > 0) {
         batch_child_records_kernel<<<grid_blocks(2LL * n_merge_items, kThreads), kThreads, 0, s>>>(
-            sc, nodes, merge_items, n_merge_items, arena, reinterpret_cast<ChildRec*>(crecs));
+            sc, nodes, tables, merge_items, n_merge_items, arena, reinterpret_cast<ChildRec*>(crecs));
         note_launches(1);
         if (int st = check_launch("batch_child_records")) return st;
     }
@@ -2106,7 +2164,7 @@ int launch_split_evaluate_lattice(const float2* image, const PolarDesc& grid, co
     flat.origin[2] = flat.step_row[2] = flat.step_col[2] = 0.0;
     const int lc = 5;
     split_evaluate_lattice_kernel<<<tiles_of(lattice.rows, lattice.cols, lc), kThreads, 0, s>>>(
-        P.K, P.scale_w, P.inv_scale_w, grid, image, flat, lc, out);
+        P.Kh, P.Kl, (float)P.scale_w, (float)P.inv_scale_w, grid, image, flat, lc, out);
     note_launches(1);
     return check_launch("split_evaluate_lattice");
 }

@@ -100,6 +100,7 @@ int sarbp_direct_polar_static(const float* data, int pulses, int samples, const 
     g.win_nr = grid->nr;
     g.win_nu = grid->nu;
     g.out_stride = grid->nu;
+    split_geometry(g);
     double radius = 0.0;
     g.tile_lc = split_polar_tile_lc(g, &radius);
     const int wb = split_window_bins(radius, data_dr);
