@@ -18,6 +18,12 @@
 // reduced modulo one turn without rounding.  The reduced phase feeds the
 // hardware sin/cos (MUFU) on [-pi, pi).
 //
+// Lattice tiles go further: delta_p = i s_row + j s_col, so u . delta_p and W . delta_p are
+// sums of a row and a column term.  The records carry the two terms per pulse (the phase
+// ones split exactly as above), each thread forms them once per pulse at a reference pixel,
+// and its four pixels, m rows apart, step from there: per pixel-pulse only the eps term,
+// the window gather and the rotation remain.
+//
 // Range interpolation: for each (tile, pulse) the chunk stages the range bins
 // the tile can touch as Horner coefficients of the reference's four-point
 // Lagrange cubic (weight folded in), 32 bytes per bin; a pixel-pulse is then
@@ -46,10 +52,10 @@ constexpr int kWindowBudget = 68 * 1024;
 constexpr double kDirectEnvelope = 8.0;
 
 struct Rec {
-    float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y
-    float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2
+    float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y   (lattice: B_row hi, lo, B_col hi, lo)
+    float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2       (lattice: u.s_row, u.s_col, 2R, frac(Q) - 1/2)
     float4 c;  // Phi, window bias bits, window offset bits, window count - 1 bits
-    float4 d;  // u.z, W_hi.z, W_lo.z
+    float4 d;  // u.z, W_hi.z, W_lo.z                (lattice: frac(m B_row), m u.s_row)
 };
 
 struct Pix {
@@ -76,6 +82,8 @@ struct TileShared {
     int nfit_w[2];              // fitting pulses among each record warp's 32
     unsigned miss_w[2];         // pulses of each record warp that cannot be staged (bit per lane)
     int wsum;                   // window entries of record warp 0's pulses
+    float sth[6], stl[6];       // lattice tiles: step_row (0-2) and step_col (3-5) as two-float
+    int row_step;               // lattice tiles: rows between a thread's successive pixels
 };
 
 // Row/column tables of a polar tile; aliased onto the window region during set-up.
@@ -162,6 +170,12 @@ __device__ __forceinline__ void block_sum4(TileShared& S, double v[4]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) v[i] = S.sum[i];
     __syncthreads();
+}
+
+// v as an unevaluated sum h + l of two FP32 numbers.
+__device__ __forceinline__ void split2(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
 }
 
 __device__ __forceinline__ void set_quantum(TileShared& S, float bound, int bits) {
@@ -408,6 +422,46 @@ __device__ void setup_lattice(const Job& J, TileShared& S, Pix px[kPX]) {
     }
 }
 
+// Lattice tile set-up for the separable pulse loop: the tile centre, bounds and quantum as
+// setup_lattice, the steps as two-float, and per pixel only |delta|^2 (FP32).  Thread t holds
+// pixels (row (t >> lc) + k m, column t & (cols - 1)), k = 0..3, m = kThreads >> lc.
+__device__ void setup_lattice_sep(const Job& J, TileShared& S, float d2[kPX]) {
+    const sarbp_lattice& L = J.lat;
+    const int tid = threadIdx.x;
+    const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
+    const int hr = rows_t >> 1, hc = cols_t >> 1;
+    if (tid == 0) {
+        const double i0 = (double)(J.tile_r + hr), j0 = (double)(J.tile_u + hc);
+        S.cx = L.origin[0] + i0 * L.step_row[0] + j0 * L.step_col[0];
+        S.cy = L.origin[1] + i0 * L.step_row[1] + j0 * L.step_col[1];
+        S.cz = L.origin[2] + i0 * L.step_row[2] + j0 * L.step_col[2];
+        double b[3];
+        for (int c = 0; c < 3; ++c) {
+            b[c] = hr * fabs(L.step_row[c]) + hc * fabs(L.step_col[c]);
+            split2(L.step_row[c], S.sth[c], S.stl[c]);
+            split2(L.step_col[c], S.sth[3 + c], S.stl[3 + c]);
+        }
+        S.rho = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) * 1.0001 + 1e-6;
+        for (int c = 0; c < 3; ++c) S.bnd[c] = (float)(b[c] * 1.0001 + 1e-6);
+        const bool has_z = L.step_row[2] != 0.0 || L.step_col[2] != 0.0;
+        set_quantum(S, (float)(fmax(b[0], fmax(b[1], b[2])) * 1.0001 + 1e-6), has_z ? 11 : 12);
+        S.row_step = kThreads >> J.lc;
+    }
+    __syncthreads();
+    const float dj = (float)((tid & (cols_t - 1)) - hc);
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const float di = (float)(((tid + kThreads * k) >> J.lc) - hr);
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float x = fmaf(di, S.sth[c], dj * S.sth[3 + c]);
+            v = fmaf(x, x, v);
+        }
+        d2[k] = v;
+    }
+}
+
 __device__ void setup_points(const Job& J, TileShared& S, Pix px[kPX]) {
     const int tid = threadIdx.x;
     double p3[kPX][3];
@@ -596,11 +650,6 @@ __device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* s
 // a chunk that stages no window live at the start of the window space.
 __host__ __device__ constexpr size_t window_offset() { return (size_t)kMaxChunk * sizeof(Rec); }
 
-__device__ __forceinline__ void split2(double v, float& h, float& l) {
-    h = (float)v;
-    l = (float)(v - (double)h);
-}
-
 // Range-sample value and its derivative for a pixel at offset delta from the tile centre,
 // pulse record sr, in two-float geometry: returns false when the taps leave the row.
 struct SlowSample {
@@ -672,6 +721,7 @@ __device__ __noinline__ void slow_record(const SplitParams& P, const TileShared&
 // arithmetic (about 44 bits; GB300's FP64 rate would make these records the barrier-bound
 // part of every chunk).  Returns the number of window entries the pulse needs (cap + 1 if
 // it cannot be staged).
+template <bool SEP>
 __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, Rec* rec, int lane, int n) {
     const PulseInputs& in = P.in;
     float ph_, pl_;
@@ -714,20 +764,45 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
     const int bo = ok ? (int)lo : 0;
     S.base[lane] = ok ? (int)I + bo : 0;
     S.wt[lane] = (float)in.weight[n];
-    const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
     Rec r;
     const FF Wx = ff_mul(Kk, ux), Wy = ff_mul(Kk, uy), Wz = ff_mul(Kk, uz);
-    r.a.x = rintf(Wx.h * isw) * sw;
-    r.a.z = (Wx.h - r.a.x) + Wx.l;
-    r.a.y = rintf(Wy.h * isw) * sw;
-    r.a.w = (Wy.h - r.a.y) + Wy.l;
-    r.d.y = rintf(Wz.h * isw) * sw;
-    r.d.z = (Wz.h - r.d.y) + Wz.l;
-    r.b = make_float4(uxf, uyf, 2.0f * Rf, Fm);
+    if (SEP) {
+        // Lattice tile: the linear phase W . delta of pixel (i, j) is i B_row + j B_col with
+        // B = W . step.  Both are split on one power-of-two quantum with <= 10 significant
+        // bits, so i B_row_hi + j B_col_hi is exact in FP32 for |i|, |j| < 2^12.
+        const FF Br = ff_add(ff_add(ff_mul(Wx, FF{S.sth[0], S.stl[0]}), ff_mul(Wy, FF{S.sth[1], S.stl[1]})),
+                             ff_mul(Wz, FF{S.sth[2], S.stl[2]}));
+        const FF Bc = ff_add(ff_add(ff_mul(Wx, FF{S.sth[3], S.stl[3]}), ff_mul(Wy, FF{S.sth[4], S.stl[4]})),
+                             ff_mul(Wz, FF{S.sth[5], S.stl[5]}));
+        const int e = ((__float_as_int(fmaxf(fmaxf(fabsf(Br.h), fabsf(Bc.h)), 1e-30f)) >> 23) & 0xff) - 126;
+        const float q = __int_as_float((e - 10 + 127) << 23), iq = __int_as_float((10 - e + 127) << 23);
+        r.a.x = rintf(Br.h * iq) * q;
+        r.a.y = (Br.h - r.a.x) + Br.l;
+        r.a.z = rintf(Bc.h * iq) * q;
+        r.a.w = (Bc.h - r.a.z) + Bc.l;
+        // Phase and range steps between a thread's successive pixels (m = kThreads >> lc rows).
+        const float m = (float)S.row_step;
+        const float mh = m * Br.h;  // exact: m is a power of two
+        float sp = (mh - rintf(mh)) + m * Br.l;
+        sp -= rintf(sp);
+        const float Ar = fmaf(uxf, S.sth[0], fmaf(uyf, S.sth[1], uzf * S.sth[2]));
+        const float Ac = fmaf(uxf, S.sth[3], fmaf(uyf, S.sth[4], uzf * S.sth[5]));
+        r.b = make_float4(Ar, Ac, 2.0f * Rf, Fm);
+        r.d = make_float4(sp, m * Ar, 0.0f, 0.0f);
+    } else {
+        const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
+        r.a.x = rintf(Wx.h * isw) * sw;
+        r.a.z = (Wx.h - r.a.x) + Wx.l;
+        r.a.y = rintf(Wy.h * isw) * sw;
+        r.a.w = (Wy.h - r.a.y) + Wy.l;
+        r.d.y = rintf(Wz.h * isw) * sw;
+        r.d.z = (Wz.h - r.d.y) + Wz.l;
+        r.b = make_float4(uxf, uyf, 2.0f * Rf, Fm);
+        r.d.x = uzf;
+        r.d.w = 0.0f;
+    }
     r.c.x = t1;
     r.c.y = __int_as_float(kMagicBits + bo);
-    r.d.x = uzf;
-    r.d.w = 0.0f;
     const int count = ok ? (int)(hi - lo) + 1 : P.cap + 1;
     r.c.z = 0.0f;
     r.c.w = __int_as_float(count - 1);
@@ -782,7 +857,7 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
         __syncthreads();  // the previous chunk's records and windows are consumed
         if (warp < 2) {
             const int idx = 32 * warp + lane;
-            const int count = idx < want ? make_record(P, S, rec, idx, c0 + idx) : 0;
+            const int count = idx < want ? make_record<Body::kSep>(P, S, rec, idx, c0 + idx) : 0;
             int inc = count;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -842,6 +917,7 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 
 template <bool HAS_Z, bool DEMOD>
 struct ForwardBody {
+    static constexpr bool kSep = false;
     const SplitParams& P;
     const TileShared& S;
     Pix* px;
@@ -864,6 +940,88 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
     chunk_loop(P, J, S, smem, true, body);
 }
 
+// ---- lattice tiles: separable pulse loop ------------------------------------------------
+//
+// On a lattice the pixel offset is delta = i s_row + j s_col, so u . delta and W . delta
+// split into row and column terms.  Per (thread, pulse) the record gives the terms at the
+// thread's reference pixel (row (t >> lc) + 2m, its column): L0 = u . delta, and the phase
+// r0 = frac(Phi + W . delta) from the exact hi products; its other pixels are kc = -2..1
+// steps of m rows away, L = L0 + kc (m u . s_row) and phase r0 + kc frac(m W . s_row).
+// Per pixel-pulse this leaves the eps term, the window gather and the rotation.
+__device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* __restrict__ rec,
+                                              const float4* __restrict__ win, int chn, int lc, const float d2[kPX],
+                                              float ar[kPX], float ai[kPX]) {
+    const float inv_dr = P.inv_drf, Kf = P.Kf;
+    const int m = kThreads >> lc, hr = (kSplitTilePixels >> lc) >> 1, cols_t = 1 << lc;
+    const int tid = threadIdx.x;
+    const float di = (float)((tid >> lc) + 2 * m - hr);
+    const float dj = (float)((tid & (cols_t - 1)) - (cols_t >> 1));
+#pragma unroll 1
+    for (int nl = 0; nl < chn; ++nl) {
+        const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+        const int bias = __float_as_int(rc.y);
+        const unsigned last = (unsigned)__float_as_int(rc.w);
+        const float4* wrow = win + 2 * __float_as_int(rc.z);
+        const float L0 = fmaf(dj, rb.y, di * rb.x);
+        const float t = fmaf(dj, ra.z, di * ra.x);  // exact
+        const float r0 = (t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x));
+#pragma unroll
+        for (int k = 0; k < kPX; ++k) {
+            const float kc = (float)(k - 2);
+            const float L = fmaf(kc, rd.y, L0);
+            const float q2 = fmaf(-L, L, d2[k]);
+            const float B = rcp_approx(fmaf(2.0f, L, rb.z));
+            const float e0 = q2 * B;
+            const float eps = fmaf(-e0 * e0, B, e0);
+            const float qp = fmaf(L + eps, inv_dr, rb.w);
+            const float tq = qp + kMagic;
+            const float s = qp - (tq - kMagic);
+            const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
+            const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+            const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+            const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+            // |r0| <= 1/2 + small, |kc frac| <= 1 and K eps <= envelope / 2 turns: the angle
+            // stays within +-40 rad, which the hardware sin/cos reduce themselves.
+            const float ang = fmaf(Kf, eps, fmaf(kc, rd.x, r0)) * kTwoPiF;
+            float sn, cs;
+            __sincosf(ang, &sn, &cs);
+            ar[k] = fmaf(vr, cs, ar[k]);
+            ar[k] = fmaf(-vi, sn, ar[k]);
+            ai[k] = fmaf(vr, sn, ai[k]);
+            ai[k] = fmaf(vi, cs, ai[k]);
+        }
+    }
+}
+
+struct LatticeBody {
+    static constexpr bool kSep = true;
+    const SplitParams& P;
+    const TileShared& S;
+    const Job& J;
+    const float* d2;
+    float* ar;
+    float* ai;
+    __device__ void fast(const Rec* rec, const float4* win, int nfit, int) {
+        lattice_chunk(P, rec, win, nfit, J.lc, d2, ar, ai);
+    }
+    // Pulses the fast path cannot stage: the pixel offsets in two-float from FP64 (rare).
+    __device__ void slow(int c0, int nslow, const SlowRec* srec) {
+        const sarbp_lattice& L = J.lat;
+        const int tid = threadIdx.x, cols_t = 1 << J.lc, hr = (kSplitTilePixels >> J.lc) >> 1;
+        const double dj = (double)((tid & (cols_t - 1)) - (cols_t >> 1));
+#pragma unroll 1
+        for (int k = 0; k < kPX; ++k) {
+            const double di = (double)(((tid + kThreads * k) >> J.lc) - hr);
+            Pix q;
+            pixel_from_offsets(S, di * L.step_row[0] + dj * L.step_col[0], di * L.step_row[1] + dj * L.step_col[1],
+                               di * L.step_row[2] + dj * L.step_col[2], q);
+            const float2 v = slow_pixel(P, srec, nslow, c0, q.dxh, q.dxl, q.dyh, q.dyl, q.dzh, q.dzl, 0.0f);
+            ar[k] += v.x;
+            ai[k] += v.y;
+        }
+    }
+};
+
 // ---- adjoint (gradients of a real image loss) -------------------------------------------
 //
 // With G_p = dl/dRe I_p + i dl/dIm I_p and c_pn = w_n v_pn exp(i phi_pn), the
@@ -877,6 +1035,7 @@ constexpr int kAdjVals = 5;  // Re U, Im U, A.x, A.y, A.z
 
 template <bool HAS_Z, bool DEMOD>
 struct AdjointBody {
+    static constexpr bool kSep = false;
     const SplitParams& P;
     const TileShared& S;
     Pix* px;
@@ -1052,7 +1211,6 @@ __global__ void __launch_bounds__(kThreads, 3) split_polar_kernel(SplitParams P,
 
 // One lattice tile over pulses [p0, p1): the per-item body shared by the one-tile-per-CTA
 // kernel and the persistent batch kernel.
-template <bool HAS_Z>
 __device__ __forceinline__ void lattice_tile(const SplitParams& P, const sarbp_lattice& lat, int lc, int tile_r,
                                              int tile_u, int p0, int p1, float2* out, TileShared& S, char* smem) {
     Job J;
@@ -1062,20 +1220,28 @@ __device__ __forceinline__ void lattice_tile(const SplitParams& P, const sarbp_l
     J.tile_u = tile_u;
     J.p0 = p0;
     J.p1 = p1;
-    Pix px[kPX];
-    setup_lattice<HAS_Z>(J, S, px);
-    pulse_loop<HAS_Z, false>(P, J, S, smem, px);
-    store_window(J, lat.rows, lat.cols, px, out, lat.cols);
+    float d2[kPX], ar[kPX], ai[kPX];
+    setup_lattice_sep(J, S, d2);
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) ar[k] = ai[k] = 0.0f;
+    LatticeBody body{P, S, J, d2, ar, ai};
+    chunk_loop(P, J, S, smem, true, body);
+    const int cols_t = 1 << lc;
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const int p = threadIdx.x + kThreads * k;
+        const int wr = tile_r + (p >> lc), wu = tile_u + (p & (cols_t - 1));
+        if (wr < lat.rows && wu < lat.cols) out[(long long)wr * lat.cols + wu] = make_float2(ar[k], ai[k]);
+    }
 }
 
-template <bool HAS_Z>
 __global__ void __launch_bounds__(kThreads, 3) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     int tile_r, tile_u, p0, p1;
     tile_of(blockIdx.x, lat.cols, lc, tile_r, tile_u);
     split_range(0, P.in.pulses, P.pulse_split, blockIdx.y, p0, p1);
-    lattice_tile<HAS_Z>(P, lat, lc, tile_r, tile_u, p0, p1, P.out + blockIdx.y * P.split_stride, S, smem);
+    lattice_tile(P, lat, lc, tile_r, tile_u, p0, p1, P.out + blockIdx.y * P.split_stride, S, smem);
 }
 
 __global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P, const double* __restrict__ xyz,
@@ -1786,14 +1952,8 @@ int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pu
     const int lc = 5;
     const size_t smem = dynamic_smem(P.cap, false);
     dim3 grid(tiles_of(lat.rows, lat.cols, lc), pulse_split);
-    const bool has_z = lat.step_row[2] != 0.0 || lat.step_col[2] != 0.0;
-    if (has_z) {
-        if (int st = prepare(split_lattice_kernel<true>, smem)) return st;
-        split_lattice_kernel<true><<<grid, kThreads, smem, s>>>(P, lat, lc);
-    } else {
-        if (int st = prepare(split_lattice_kernel<false>, smem)) return st;
-        split_lattice_kernel<false><<<grid, kThreads, smem, s>>>(P, lat, lc);
-    }
+    if (int st = prepare(split_lattice_kernel, smem)) return st;
+    split_lattice_kernel<<<grid, kThreads, smem, s>>>(P, lat, lc);
     note_launches(1);
     return check_launch("split_lattice");
 }
@@ -1992,7 +2152,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_direct_kernel(const BatchSc
             load_scene(scenes, it.pad, sc);
             if (threadIdx.x == 0) s_scene = it.pad;
         }
-        lattice_tile<false>(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
+        lattice_tile(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
     }
 }
 
