@@ -47,6 +47,10 @@ constexpr int kMaxChunk = 64;      // pulses per chunk of the direct kernels: tw
 constexpr int kMaxLeafChunk = 32;  // pulses per chunk of the FFBP leaf kernels: one warp computes the records
 // Window bytes per CTA: with kMaxChunk records this keeps three CTAs per SM within 227 KB.
 constexpr int kWindowBudget = 68 * 1024;
+// Lattice tiles (64 registers): four CTAs per SM.  The packed windows of a 32 x 32 tile at the
+// usual geometries need 15-25 bins per pulse, so 64-pulse chunks still fit; wider windows
+// just fit fewer pulses per chunk.
+constexpr int kLatticeWindowBudget = 50 * 1024;
 // K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
 // error, FFBP leaves 1e-4.
 constexpr double kDirectEnvelope = 8.0;
@@ -788,7 +792,7 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
         const float Ar = fmaf(uxf, S.sth[0], fmaf(uyf, S.sth[1], uzf * S.sth[2]));
         const float Ac = fmaf(uxf, S.sth[3], fmaf(uyf, S.sth[4], uzf * S.sth[5]));
         r.b = make_float4(Ar, Ac, 2.0f * Rf, Fm);
-        r.d = make_float4(sp, m * Ar, 0.0f, 0.0f);
+        r.d = make_float4(sp * kTwoPiF, m * Ar, 0.0f, 0.0f);  // the phase step in radians
     } else {
         const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
         r.a.x = rintf(Wx.h * isw) * sw;
@@ -951,7 +955,7 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 __device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* __restrict__ rec,
                                               const float4* __restrict__ win, int chn, int lc, const float d2[kPX],
                                               float ar[kPX], float ai[kPX]) {
-    const float inv_dr = P.inv_drf, Kf = P.Kf;
+    const float inv_dr = P.inv_drf, kr = P.Kf * kTwoPiF;
     const int m = kThreads >> lc, hr = (kSplitTilePixels >> lc) >> 1, cols_t = 1 << lc;
     const int tid = threadIdx.x;
     const float di = (float)((tid >> lc) + 2 * m - hr);
@@ -964,7 +968,7 @@ __device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* _
         const float4* wrow = win + 2 * __float_as_int(rc.z);
         const float L0 = fmaf(dj, rb.y, di * rb.x);
         const float t = fmaf(dj, ra.z, di * ra.x);  // exact
-        const float r0 = (t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x));
+        const float r0 = ((t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x))) * kTwoPiF;  // radians
 #pragma unroll
         for (int k = 0; k < kPX; ++k) {
             const float kc = (float)(k - 2);
@@ -982,7 +986,7 @@ __device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* _
             const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
             // |r0| <= 1/2 + small, |kc frac| <= 1 and K eps <= envelope / 2 turns: the angle
             // stays within +-40 rad, which the hardware sin/cos reduce themselves.
-            const float ang = fmaf(Kf, eps, fmaf(kc, rd.x, r0)) * kTwoPiF;
+            const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
             float sn, cs;
             __sincosf(ang, &sn, &cs);
             ar[k] = fmaf(vr, cs, ar[k]);
@@ -1235,7 +1239,7 @@ __device__ __forceinline__ void lattice_tile(const SplitParams& P, const sarbp_l
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 3) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
+__global__ void __launch_bounds__(kThreads, 4) split_lattice_kernel(SplitParams P, sarbp_lattice lat, int lc) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     int tile_r, tile_u, p0, p1;
@@ -1883,9 +1887,9 @@ int tiles_of(int nr, int nu, int lc) {
 
 // Window entries for one chunk: `chunk` pulses whose windows span at most
 // `window_bins` bins each (the kernel packs the actual, usually smaller, windows).
-int capacity_for(int chunk, int window_bins) {
+int capacity_for(int chunk, int window_bins, int budget_bytes = kWindowBudget) {
     long long cap = (long long)chunk * window_bins;
-    const long long budget = kWindowBudget / 32;
+    const long long budget = budget_bytes / 32;
     return (int)(cap > budget ? budget : cap);
 }
 
@@ -1946,7 +1950,7 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
 
 int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk, int window_bins,
                          float2* out, long long split_stride, cudaStream_t s) {
-    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), pulse_split);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins, kLatticeWindowBudget), pulse_split);
     P.out = out;
     P.split_stride = split_stride;
     const int lc = 5;
@@ -2116,8 +2120,7 @@ struct BatchScene {
     sarbp_lattice lat;      // direct scenes
     int kind;               // 0 direct lattice, 1 FFBP
     int lc;                 // direct: log2 of tile columns
-    int has_z;
-    int pad;
+    int pad[2];
     long long prec_offset;  // FFBP: first pulse record of the scene
 };
 
@@ -2136,7 +2139,7 @@ __device__ __forceinline__ void load_scene(const BatchScene* __restrict__ scenes
 }
 
 // Direct tiles of every direct scene (flat lattices only, checked when the batch is created).
-__global__ void __launch_bounds__(kThreads, 3) batch_direct_kernel(const BatchScene* __restrict__ scenes,
+__global__ void __launch_bounds__(kThreads, 4) batch_direct_kernel(const BatchScene* __restrict__ scenes,
                                                                    const TileItem* __restrict__ items, int nitems,
                                                                    int* counter) {
     extern __shared__ __align__(16) char smem[];
@@ -2230,12 +2233,14 @@ size_t split_batch_scene_bytes() { return sizeof(BatchScene); }
 
 size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     BatchScene b{};
-    b.P = make_params(d.in, d.chunk, capacity_for(d.chunk, d.window_bins), 1);
+    b.P = make_params(d.in, d.chunk,
+                      d.kind == 0 ? capacity_for(d.chunk, d.window_bins, kLatticeWindowBudget)
+                                  : capacity_for(d.chunk, d.window_bins),
+                      1);
     b.P.out = d.out;
     b.lat = d.lat;
     b.kind = d.kind;
     b.lc = d.lc;
-    b.has_z = (d.lat.step_row[2] != 0.0 || d.lat.step_col[2] != 0.0) ? 1 : 0;
     b.prec_offset = d.prec_offset;
     memcpy(dst, &b, sizeof(b));
     return (d.kind == 0 ? window_offset() : (size_t)kMaxLeafChunk * sizeof(LeafRec)) + (size_t)b.P.cap * 32;
