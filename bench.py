@@ -43,7 +43,7 @@ REF_SAMPLE_PIXELS = 131072          # pixels per step of the reference arm (~1 s
 # DRAM bytes (read + write) of one split_lattice_kernel launch on this workload, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum): only the ~920 range bins per pulse that the scene spans
 # are read, so traffic is far below the algorithmic 302 MB.
-NCU_TRAFFIC_BYTES = 31.903744e6 + 2.073344e6
+NCU_TRAFFIC_BYTES = 31.905536e6 + 3.394304e6
 
 
 def parse():

@@ -202,6 +202,34 @@ def test_ragged_and_edge_lattices_vs_fp64_oracle(lib, shape, step, tilt, shift):
         assert err <= tol
 
 
+@pytest.mark.parametrize("step", [6.0, 1.0, 0.9])
+def test_lattice_tiles_outside_the_envelope_match_fp64(lib, step):
+    """Coarse lattices whose 32 x 32 tiles are too wide for the fast path's precision envelope
+    (K rho^2 > 8 R at 6 m and 1 m spacing, windows of ~330 and ~55 bins): every pulse takes the
+    lattice tiles' two-float fallback, which must meet the split tolerance against the FP64
+    oracle.  At 0.9 m the tiles fit the envelope again (fast path, wide windows)."""
+    from bp_project_gb300 import core
+    from oracle import reference as ora
+    sc = _scene("c0", pulses=384, image_side=64)
+    lat = sc.lattice
+    rows = cols = 40
+    centre = lat.origin + 0.5 * lat.rows * lat.step_row + 0.5 * lat.cols * lat.step_col
+    origin = tuple(centre - 0.5 * step * np.array([rows, cols, 0.0]))
+    srow, scol = (step, 0.0, 0.0), (0.0, step, 0.0)
+    i = np.arange(rows)[:, None, None]
+    j = np.arange(cols)[None, :, None]
+    pts = (np.array(origin) + i * np.array(srow) + j * np.array(scol)).reshape(-1, 3)
+    _, ref = ora.backproject_points(sc.data, sc.position, pts, sc.range_start, sc.data_dr, sc.k, sc.weight, sc.phase,
+                                    c128=True)
+    args = [_dev(a, dt) for a, dt in ((sc.data, torch.complex64), (sc.position, torch.float64),
+                                      (sc.weight, torch.float64), (sc.phase, torch.float64))]
+    out = core.backproject_lattice(*args, origin, srow, scol, rows, cols, sc.range_start, sc.data_dr, sc.k,
+                                   mode="split").cpu().numpy().ravel()
+    err = rel_err(ref, out)
+    print(f"lattice step {step} m (two-float fallback tiles): {err:.2e}")
+    assert err <= 1e-5
+
+
 def test_points_outside_the_envelope_match_fp64(lib):
     """Points scattered over the whole scene: every 1024-point tile is too wide for the split
     path's precision envelope, so every pulse takes the two-float fallback; it must still meet
