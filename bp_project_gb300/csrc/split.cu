@@ -59,7 +59,7 @@ struct Rec {
     float4 a;  // W_hi.x, W_hi.y, W_lo.x, W_lo.y   (lattice: B_row hi, lo, B_col hi, lo)
     float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2       (lattice: u.s_row, u.s_col, 2R, frac(Q) - 1/2)
     float4 c;  // Phi, window bias bits, window offset bits, window count - 1 bits
-    float4 d;  // u.z, W_hi.z, W_lo.z                (lattice: frac(m B_row), m u.s_row)
+    float4 d;  // u.z, W_hi.z, W_lo.z                (lattice: 2 pi frac(m B_row), m u.s_row or u.x, u.y, u.z)
 };
 
 struct Pix {
@@ -725,7 +725,8 @@ __device__ __noinline__ void slow_record(const SplitParams& P, const TileShared&
 // arithmetic (about 44 bits; GB300's FP64 rate would make these records the barrier-bound
 // part of every chunk).  Returns the number of window entries the pulse needs (cap + 1 if
 // it cannot be staged).
-template <bool SEP>
+// MODE 0: per-pixel offsets (polar, points); 1: lattice tiles; 2: lattice tiles, adjoint.
+template <int MODE>
 __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, Rec* rec, int lane, int n) {
     const PulseInputs& in = P.in;
     float ph_, pl_;
@@ -770,7 +771,7 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
     S.wt[lane] = (float)in.weight[n];
     Rec r;
     const FF Wx = ff_mul(Kk, ux), Wy = ff_mul(Kk, uy), Wz = ff_mul(Kk, uz);
-    if (SEP) {
+    if (MODE != 0) {
         // Lattice tile: the linear phase W . delta of pixel (i, j) is i B_row + j B_col with
         // B = W . step.  Both are split on one power-of-two quantum with <= 10 significant
         // bits, so i B_row_hi + j B_col_hi is exact in FP32 for |i|, |j| < 2^12.
@@ -792,7 +793,8 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
         const float Ar = fmaf(uxf, S.sth[0], fmaf(uyf, S.sth[1], uzf * S.sth[2]));
         const float Ac = fmaf(uxf, S.sth[3], fmaf(uyf, S.sth[4], uzf * S.sth[5]));
         r.b = make_float4(Ar, Ac, 2.0f * Rf, Fm);
-        r.d = make_float4(sp * kTwoPiF, m * Ar, 0.0f, 0.0f);  // the phase step in radians
+        // The phase step in radians; the range step (forward) or u (adjoint).
+        r.d = MODE == 1 ? make_float4(sp * kTwoPiF, m * Ar, 0.0f, 0.0f) : make_float4(sp * kTwoPiF, uxf, uyf, uzf);
     } else {
         const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
         r.a.x = rintf(Wx.h * isw) * sw;
@@ -861,7 +863,7 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
         __syncthreads();  // the previous chunk's records and windows are consumed
         if (warp < 2) {
             const int idx = 32 * warp + lane;
-            const int count = idx < want ? make_record<Body::kSep>(P, S, rec, idx, c0 + idx) : 0;
+            const int count = idx < want ? make_record<Body::kRecMode>(P, S, rec, idx, c0 + idx) : 0;
             int inc = count;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -921,7 +923,7 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 
 template <bool HAS_Z, bool DEMOD>
 struct ForwardBody {
-    static constexpr bool kSep = false;
+    static constexpr int kRecMode = 0;
     const SplitParams& P;
     const TileShared& S;
     Pix* px;
@@ -998,7 +1000,7 @@ __device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* _
 }
 
 struct LatticeBody {
-    static constexpr bool kSep = true;
+    static constexpr int kRecMode = 1;
     const SplitParams& P;
     const TileShared& S;
     const Job& J;
@@ -1039,7 +1041,7 @@ constexpr int kAdjVals = 5;  // Re U, Im U, A.x, A.y, A.z
 
 template <bool HAS_Z, bool DEMOD>
 struct AdjointBody {
-    static constexpr bool kSep = false;
+    static constexpr int kRecMode = 0;
     const SplitParams& P;
     const TileShared& S;
     Pix* px;
@@ -1172,6 +1174,133 @@ struct AdjointBody {
     }
 };
 
+// Adjoint on lattice tiles, with the forward's separable row/column terms.  Per pulse a
+// thread sums its pixels' t_p = Re(conj(G_p) z_p e^{i phi}) / d_p as T0 = sum t_p and
+// S1 = sum kc_p t_p; with delta_p = di_p s_row + dj_p s_col the position sum is
+// A = sum t_p (R u + delta_p) = R u T0 + s_row Ti + s_col Tj, Ti = sum t_p di_p = di T0 + m S1,
+// Tj = dj T0 (a thread's pixels share the column).  The warps reduce (Re U, Im U, T0, Ti, Tj)
+// and the flush turns them into A with the chunk's records.
+__device__ __noinline__ void lattice_adjoint_slow(const SplitParams& P, const TileShared& S, const Job& J, float g0,
+                                                  float g1, float g2, float g3, float h0, float h1, float h2,
+                                                  float h3, float (*red)[kMaxChunk][kAdjVals], float* part, int c0,
+                                                  int nslow, const SlowRec* srec) {
+    const sarbp_lattice& L = J.lat;
+    const int tid = threadIdx.x, cols_t = 1 << J.lc, hr = (kSplitTilePixels >> J.lc) >> 1;
+    const double dj = (double)((tid & (cols_t - 1)) - (cols_t >> 1));
+    Pix px[kPX];
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) {
+        const double di = (double)(((tid + kThreads * k) >> J.lc) - hr);
+        pixel_from_offsets(S, di * L.step_row[0] + dj * L.step_col[0], di * L.step_row[1] + dj * L.step_col[1],
+                           di * L.step_row[2] + dj * L.step_col[2], px[k]);
+        px[k].psi = 0.0f;
+    }
+    const float gre[kPX] = {g0, g1, g2, g3}, gim[kPX] = {h0, h1, h2, h3};
+    AdjointBody<true, false> body{P, S, px, gre, gim, red, part, kSplitTilePixels};
+    body.slow(c0, nslow, srec);  // writes A directly
+}
+
+struct LatticeAdjointBody {
+    static constexpr int kRecMode = 2;
+    const SplitParams& P;
+    const TileShared& S;
+    const Job& J;
+    const float* d2;
+    const float* gre;
+    const float* gim;
+    float (*red)[kMaxChunk][kAdjVals];
+    float* part;
+
+    __device__ void flush(int n0, int cnt, const Rec* rec) {
+        __syncthreads();
+        for (int nl = threadIdx.x; nl < cnt; nl += kThreads) {
+            float v[kAdjVals];
+#pragma unroll
+            for (int c = 0; c < kAdjVals; ++c) {
+                float acc = 0.0f;
+#pragma unroll
+                for (int w = 0; w < kThreads / 32; ++w) acc += red[w][nl][c];
+                v[c] = acc;
+            }
+            const float4 rd = rec[nl].d;
+            const float R = 0.5f * rec[nl].b.z, t0 = v[2], ti = v[3], tj = v[4];
+            const float u[3] = {rd.y, rd.z, rd.w};
+            float* out = part + (size_t)(n0 + nl) * kAdjVals;
+            out[0] = v[0];
+            out[1] = v[1];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) out[2 + c] = fmaf(R * u[c], t0, fmaf(S.sth[c], ti, S.sth[3 + c] * tj));
+        }
+    }
+
+    __device__ void fast(const Rec* rec, const float4* win, int nfit, int c0) {
+        const float inv_dr = P.inv_drf, kr = P.Kf * kTwoPiF;
+        const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, lc = J.lc;
+        const int m = kThreads >> lc, hr = (kSplitTilePixels >> lc) >> 1, cols_t = 1 << lc;
+        const float di = (float)((tid >> lc) + 2 * m - hr);
+        const float dj = (float)((tid & (cols_t - 1)) - (cols_t >> 1));
+        const float mf = (float)m;
+#pragma unroll 1
+        for (int nl = 0; nl < nfit; ++nl) {
+            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+            const int bias = __float_as_int(rc.y);
+            const unsigned last = (unsigned)__float_as_int(rc.w);
+            const float4* wrow = win + 2 * __float_as_int(rc.z);
+            const float L0 = fmaf(dj, rb.y, di * rb.x), mA = mf * rb.x;
+            const float t = fmaf(dj, ra.z, di * ra.x);  // exact
+            const float r0 = ((t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x))) * kTwoPiF;
+            const float R = 0.5f * rb.z;
+            float u0 = 0.f, u1 = 0.f, t0 = 0.f, s1 = 0.f;
+#pragma unroll
+            for (int k = 0; k < kPX; ++k) {
+                const float kc = (float)(k - 2);
+                const float L = fmaf(kc, mA, L0);
+                const float q2 = fmaf(-L, L, d2[k]);
+                const float B = rcp_approx(fmaf(2.0f, L, rb.z));
+                const float e0 = q2 * B;
+                const float eps = fmaf(-e0 * e0, B, e0);
+                const float qp = fmaf(L + eps, inv_dr, rb.w);
+                const float tq = qp + kMagic;
+                const float s = qp - (tq - kMagic);
+                const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
+                const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
+                const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+                const float dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
+                const float dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
+                const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
+                float sn, cs;
+                __sincosf(ang, &sn, &cs);
+                const float gr = gre[k], gi = gim[k];
+                const float er = vr * cs - vi * sn, ei = vr * sn + vi * cs;  // v exp(i phi)
+                u0 = fmaf(gr, er, fmaf(gi, ei, u0));
+                u1 = fmaf(gr, ei, fmaf(-gi, er, u1));
+                const float zr = fmaf(dvr, inv_dr, -kr * vi), zi = fmaf(dvi, inv_dr, kr * vr);
+                const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
+                const float tt = fmaf(gr, fr, gi * fi) * rcp_approx(R + L + eps);
+                t0 += tt;
+                s1 = fmaf(kc, tt, s1);
+            }
+            float v5[kAdjVals] = {u0, u1, t0, fmaf(di, t0, mf * s1), dj * t0};
+#pragma unroll
+            for (int v = 0; v < kAdjVals; ++v) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v5[v] += __shfl_xor_sync(0xffffffffu, v5[v], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int v = 0; v < kAdjVals; ++v) red[warp][nl][v] = v5[v];
+            }
+        }
+        flush(c0, nfit, rec);
+    }
+
+    __device__ void slow(int c0, int nslow, const SlowRec* srec) {
+        lattice_adjoint_slow(P, S, J, gre[0], gre[1], gre[2], gre[3], gim[0], gim[1], gim[2], gim[3], red, part, c0,
+                             nslow, srec);
+    }
+};
+
 // ---- output ----------------------------------------------------------------------
 __device__ __forceinline__ void store_window(const Job& J, int win_nr, int win_nu, const Pix px[kPX], float2* out,
                                              long long stride) {
@@ -1271,8 +1400,7 @@ __global__ void __launch_bounds__(kThreads, 3) split_points_kernel(SplitParams P
 }
 
 // ---- adjoint kernels ----------------------------------------------------------------------
-template <bool HAS_Z>
-__global__ void __launch_bounds__(kThreads, 2) split_lattice_adjoint_kernel(SplitParams P, sarbp_lattice lat, int lc,
+__global__ void __launch_bounds__(kThreads, 3) split_lattice_adjoint_kernel(SplitParams P, sarbp_lattice lat, int lc,
                                                                             const float2* __restrict__ grad,
                                                                             float* __restrict__ partials) {
     extern __shared__ __align__(16) char smem[];
@@ -1284,9 +1412,8 @@ __global__ void __launch_bounds__(kThreads, 2) split_lattice_adjoint_kernel(Spli
     tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
     J.p0 = 0;
     J.p1 = P.in.pulses;
-    Pix px[kPX];
-    setup_lattice<HAS_Z>(J, S, px);
-    float gre[kPX], gim[kPX];
+    float d2[kPX], gre[kPX], gim[kPX];
+    setup_lattice_sep(J, S, d2);
     const int cols_t = 1 << lc;
 #pragma unroll
     for (int k = 0; k < kPX; ++k) {
@@ -1297,8 +1424,7 @@ __global__ void __launch_bounds__(kThreads, 2) split_lattice_adjoint_kernel(Spli
         gre[k] = g.x;
         gim[k] = g.y;
     }
-    AdjointBody<HAS_Z, false> body{P, S, px, gre, gim, red,
-                                   partials + (size_t)blockIdx.x * P.in.pulses * kAdjVals, kSplitTilePixels};
+    LatticeAdjointBody body{P, S, J, d2, gre, gim, red, partials + (size_t)blockIdx.x * P.in.pulses * kAdjVals};
     chunk_loop(P, J, S, smem, false, body);
 }
 
@@ -1982,18 +2108,12 @@ size_t split_adjoint_workspace(const sarbp_lattice& lat, int pulses) {
 int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat, int chunk, int window_bins,
                                  const float2* grad, float* partials, double* grad_pos, double* grad_phase,
                                  double* grad_weight, cudaStream_t s) {
-    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
+    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins, kLatticeWindowBudget), 1);
     const int lc = 5;
     const size_t smem = dynamic_smem(P.cap, false);
     const int ntiles = tiles_of(lat.rows, lat.cols, lc);
-    const bool has_z = lat.step_row[2] != 0.0 || lat.step_col[2] != 0.0;
-    if (has_z) {
-        if (int st = prepare(split_lattice_adjoint_kernel<true>, smem)) return st;
-        split_lattice_adjoint_kernel<true><<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
-    } else {
-        if (int st = prepare(split_lattice_adjoint_kernel<false>, smem)) return st;
-        split_lattice_adjoint_kernel<false><<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
-    }
+    if (int st = prepare(split_lattice_adjoint_kernel, smem)) return st;
+    split_lattice_adjoint_kernel<<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
     note_launches(1);
     if (int st = check_launch("split_lattice_adjoint")) return st;
     adjoint_sum_kernel<<<grid_blocks(in.pulses, kSumPulses), kThreads, 0, s>>>(partials, ntiles, in.pulses, in.weight,
