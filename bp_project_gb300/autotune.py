@@ -21,7 +21,7 @@ from .batch import DirectScene, SceneBatch
 
 TILE_LCS = (3, 4, 5)
 CHUNKS = (16, 32, 64)
-BLOCKS_PER_SM = (2, 3)
+BLOCKS_PER_SM = (2, 3, 4)
 DEFAULT_CACHE = Path(os.environ.get("SARBP_AUTOTUNE_CACHE", Path(__file__).resolve().parent / ".autotune.json"))
 
 
