@@ -211,7 +211,7 @@ typedef struct sarbp_batch_scene {
     int n_nodes;
     int crop_r0, crop_u0, crop_nr, crop_nu;
     int tile_lc;                  /* DIRECT: log2 of tile columns, 2..5 (tile rows = 1024 >> tile_lc); 0 = 5 */
-    int chunk_pulses;             /* pulses staged per chunk (<= 32 used); 0 = default */
+    int chunk_pulses;             /* pulses staged per chunk (DIRECT <= 64, FFBP leaves <= 32); 0 = default */
     float* out;                   /* DIRECT: complex64 [rows, cols]; FFBP: complex64 [crop_nr, crop_nu] */
 } sarbp_batch_scene;
 
