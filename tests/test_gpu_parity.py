@@ -290,6 +290,22 @@ def test_c1_direct_sampled_pixels(lib):
 
 
 @pytest.mark.slow
+def test_c2_direct_sampled_pixels(lib):
+    """Config 2 at full size (30 km, 10 GHz, 8192 x 16384, 4096^2 at 0.25 m): split lattice image vs the FP64
+    oracle on 2048 random pixels -- the long-range, fine-grid regime of the separable lattice loop."""
+    from oracle import reference as ora
+    sc = _scene("c2")
+    img = _lattice_split(sc).cpu().numpy().ravel()
+    rng = np.random.default_rng(2)
+    idx = rng.choice(img.size, 2048, replace=False)
+    ref = ora.backproject_points(sc.data, sc.position, sc.lattice.take(idx), sc.range_start, sc.data_dr, sc.k,
+                                 sc.weight, sc.phase, c128=True)[1]
+    err = rel_err(ref, img[idx])
+    print(f"c2 sampled split vs FP64: {err:.3e}")
+    assert err <= 1e-5
+
+
+@pytest.mark.slow
 def test_c1_ffbp_vs_reference_ffbp(lib):
     """Config 1 at full size: split FFBP (16-pulse leaves, 8 merge levels, root 3084 x 25031) within 1e-4 of the
     reference FFBP (oracle restatement of ffbp.form_ffbp on the same plan)."""
