@@ -49,7 +49,7 @@ class _LatticeBP(torch.autograd.Function):
         pos_c, phase_c, weight_c = pos.detach().contiguous(), phase.detach().contiguous(), weight.detach().contiguous()
         img = core.backproject_lattice(data, pos_c, weight_c, phase_c, lattice.origin, lattice.step_row,
                                        lattice.step_col, lattice.rows, lattice.cols, range_start, data_dr, k,
-                                       mode="split")
+                                       mode="split", pulse_split=0)  # 0: the split that fills the GPU
         ctx.save_for_backward(pos_c, phase_c, weight_c, data)
         ctx.geometry = (lattice, range_start, data_dr, k)
         return img

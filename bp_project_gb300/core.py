@@ -121,7 +121,10 @@ def backproject_points(data, pos, weight, phase, xyz, range_start, data_dr, k, m
 
 def backproject_lattice(data, pos, weight, phase, origin, step_row, step_col, rows, cols, range_start, data_dr, k,
                         mode=DEFAULT_MODE, pulse_split=1, out=None):
-    """Direct BP on the lattice origin + i*step_row + j*step_col -> complex64 [rows, cols]."""
+    """Direct BP on the lattice origin + i*step_row + j*step_col -> complex64 [rows, cols].
+
+    pulse_split > 1 splits each tile's pulses over that many CTAs (partial images summed in
+    fixed order); 0 lets the library pick the split that fills the GPU for this lattice."""
     p, s = check_pulses(data, pos, weight, phase)
     lat = nat.lattice(origin, step_row, step_col, rows, cols)
     if out is None:

@@ -232,8 +232,9 @@ int sarbp_backproject_points(const float* data, int pulses, int samples, const d
 }
 
 size_t sarbp_backproject_lattice_workspace(int mode, const sarbp_lattice* lattice, int pulse_split) {
-    (void)mode;
-    if (!lattice || pulse_split <= 1) return 0;
+    if (!lattice || lattice->rows <= 0 || lattice->cols <= 0) return 0;
+    if (pulse_split == 0) pulse_split = mode == SARBP_SPLIT ? split_lattice_auto_split(*lattice, 8) : 1;
+    if (pulse_split <= 1) return 0;
     return (size_t)pulse_split * (size_t)lattice->rows * (size_t)lattice->cols * sizeof(float2);
 }
 
@@ -248,8 +249,10 @@ int sarbp_backproject_lattice(const float* data, int pulses, int samples, const 
     for (int c = 0; c < 3; ++c)
         if (!is_finite_value(lattice->origin[c]) || !is_finite_value(lattice->step_row[c]) || !is_finite_value(lattice->step_col[c]))
             return fail(SARBP_ERR_VALUE, "lattice geometry must be finite");
-    if (pulse_split < 1 || pulse_split > pulses) return fail(SARBP_ERR_VALUE, "pulse_split must be in [1, pulses]");
-    if (mode != SARBP_SPLIT && pulse_split != 1) return fail(SARBP_ERR_VALUE, "pulse_split applies to split mode only");
+    if (pulse_split < 0 || pulse_split > pulses)
+        return fail(SARBP_ERR_VALUE, "pulse_split must be 0 (automatic) or in [1, pulses]");
+    if (mode != SARBP_SPLIT && pulse_split > 1) return fail(SARBP_ERR_VALUE, "pulse_split applies to split mode only");
+    if (pulse_split == 0) pulse_split = mode == SARBP_SPLIT ? split_lattice_auto_split(*lattice, pulses) : 1;
     const size_t need = sarbp_backproject_lattice_workspace(mode, lattice, pulse_split);
     if (need && (!workspace || workspace_bytes < need))
         return fail(SARBP_ERR_WORKSPACE, "backproject_lattice needs %zu workspace bytes", need);

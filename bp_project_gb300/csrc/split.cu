@@ -1410,8 +1410,7 @@ __global__ void __launch_bounds__(kThreads, 3) split_lattice_adjoint_kernel(Spli
     J.lat = lat;
     J.lc = lc;
     tile_of(blockIdx.x, lat.cols, lc, J.tile_r, J.tile_u);
-    J.p0 = 0;
-    J.p1 = P.in.pulses;
+    split_range(0, P.in.pulses, gridDim.y, blockIdx.y, J.p0, J.p1);  // the splits write disjoint partials
     float d2[kPX], gre[kPX], gim[kPX];
     setup_lattice_sep(J, S, d2);
     const int cols_t = 1 << lc;
@@ -2006,6 +2005,31 @@ int prepare(K kernel, size_t smem) {
     return SARBP_OK;
 }
 
+// Pulse split that fills the GPU's CTA slots best: the fewest waves ceil(tiles s / slots) / s over
+// s <= 8 (and <= pulses), ties to the smaller split.  A tile's pulse ranges are independent
+// work, so a small image with few tiles still keeps every SM busy to the end.
+template <class K>
+int best_pulse_split(K kernel, size_t smem, long long tiles, int pulses) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem) != cudaSuccess || per_sm <= 0 ||
+        sms <= 0 || tiles <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    const long long slots = (long long)sms * per_sm;
+    int best = 1;
+    double best_waves = 1e300;
+    for (int sp = 1; sp <= 8 && sp <= pulses; ++sp) {
+        const double waves = (double)((tiles * sp + slots - 1) / slots) / sp;
+        if (waves < best_waves - 1e-9) {
+            best_waves = waves;
+            best = sp;
+        }
+    }
+    return best;
+}
+
 int tiles_of(int nr, int nu, int lc) {
     const int cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
     return ((nr + rows_t - 1) / rows_t) * ((nu + cols_t - 1) / cols_t);
@@ -2074,6 +2098,15 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
     return check_launch("split_polar");
 }
 
+// The pulse split of a direct lattice launch that asks for the automatic one: sized for the
+// largest window budget, so that it depends on the lattice only and the workspace query and the
+// launch agree (fewer pulses only lower it).
+int split_lattice_auto_split(const sarbp_lattice& lat, int pulses) {
+    const size_t smem = dynamic_smem(kLatticeWindowBudget / 32, false);
+    if (prepare(split_lattice_kernel, smem) != SARBP_OK) return 1;
+    return best_pulse_split(split_lattice_kernel, smem, tiles_of(lat.rows, lat.cols, 5), pulses);
+}
+
 int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk, int window_bins,
                          float2* out, long long split_stride, cudaStream_t s) {
     SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins, kLatticeWindowBudget), pulse_split);
@@ -2113,7 +2146,8 @@ int launch_split_lattice_adjoint(const PulseInputs& in, const sarbp_lattice& lat
     const size_t smem = dynamic_smem(P.cap, false);
     const int ntiles = tiles_of(lat.rows, lat.cols, lc);
     if (int st = prepare(split_lattice_adjoint_kernel, smem)) return st;
-    split_lattice_adjoint_kernel<<<ntiles, kThreads, smem, s>>>(P, lat, lc, grad, partials);
+    const dim3 grid(ntiles, best_pulse_split(split_lattice_adjoint_kernel, smem, ntiles, in.pulses));
+    split_lattice_adjoint_kernel<<<grid, kThreads, smem, s>>>(P, lat, lc, grad, partials);
     note_launches(1);
     if (int st = check_launch("split_lattice_adjoint")) return st;
     adjoint_sum_kernel<<<grid_blocks(in.pulses, kSumPulses), kThreads, 0, s>>>(partials, ntiles, in.pulses, in.weight,

@@ -156,7 +156,9 @@ int sarbp_backproject_points(const float* data, int pulses, int samples, const d
                              double range_start, double data_dr, double k, int mode, int pulse_split,
                              float* out, void* workspace, size_t workspace_bytes, void* stream);
 
-/* Direct BP on an affine lattice (backproject_points semantics); out [rows, cols]. */
+/* Direct BP on an affine lattice (backproject_points semantics); out [rows, cols].
+ * pulse_split as for sarbp_direct_polar; 0 (split mode) picks the split that fills the
+ * GPU's CTA slots best for this lattice (the workspace query with 0 sizes for it). */
 size_t sarbp_backproject_lattice_workspace(int mode, const sarbp_lattice* lattice, int pulse_split);
 int sarbp_backproject_lattice(const float* data, int pulses, int samples, const double* pos,
                               const double* weight, const double* phase, const sarbp_lattice* lattice,

@@ -62,12 +62,14 @@ def torch_lattice_bp(data, pos, weight, phase, origin, step_row, step_col, rows,
     return img.reshape(rows, cols)
 
 
-def _scene(tilt):
+def _scene(tilt, coarse=1.0):
     from bp_project_gb300 import scenes
     cfg = scenes.scaled(scenes.CONFIGS["c3"], pulses=256, image_side=128)
     sc = scenes.synthesize(cfg, device="cuda")
     lat = sc.lattice
-    step_row = np.array(lat.step_row, float)
+    step_row = np.array(lat.step_row, float) * coarse
+    step_col = np.array(lat.step_col, float) * coarse
+    origin = np.array(lat.origin, float) + 0.5 * (1.0 - coarse) * lat.rows * (step_row / coarse + step_col / coarse)
     if tilt:
         step_row = step_row + np.array([0.0, 0.0, 0.05])
     rng = np.random.default_rng(7)
@@ -76,7 +78,7 @@ def _scene(tilt):
     dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a)).to("cuda", dt)
     return dict(data=dev(sc.data, torch.complex64), pos=dev(sc.position, torch.float64),
                 weight=dev(weight, torch.float64), phase=dev(phase, torch.float64),
-                origin=tuple(lat.origin), step_row=tuple(step_row), step_col=tuple(lat.step_col),
+                origin=tuple(origin), step_row=tuple(step_row), step_col=tuple(step_col),
                 rows=lat.rows, cols=lat.cols, range_start=sc.range_start, data_dr=sc.data_dr, k=sc.k)
 
 
@@ -92,10 +94,12 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("tilt", [False, True])
-def test_adjoint_matches_fp64_autograd(lib, tilt):
+@pytest.mark.parametrize("tilt,coarse", [(False, 1.0), (True, 1.0), (False, 6.0)])
+def test_adjoint_matches_fp64_autograd(lib, tilt, coarse):
+    """coarse = 6: 3 m steps, so every 32 x 32 tile is outside the fast path's precision envelope and the
+    forward and adjoint run their two-float fallbacks."""
     from bp_project_gb300.autograd import backproject_lattice
-    s = _scene(tilt)
+    s = _scene(tilt, coarse)
     geo = (s["origin"], s["step_row"], s["step_col"], s["rows"], s["cols"], s["range_start"], s["data_dr"], s["k"])
     g = torch.Generator(device="cuda").manual_seed(3)
     target = torch.randn((s["rows"], s["cols"]), dtype=torch.complex128, device="cuda", generator=g)
@@ -112,7 +116,8 @@ def test_adjoint_matches_fp64_autograd(lib, tilt):
 
     e_img = _rel(torch.view_as_real(img.detach().to(torch.complex128)), torch.view_as_real(ref_img.detach()))
     errs = [_rel(a.grad, b.grad) for a, b in zip(ins, ref_ins)]
-    print(f"tilt={tilt}: image {e_img:.2e}, grad pos {errs[0]:.2e}, phase {errs[1]:.2e}, weight {errs[2]:.2e}")
+    print(f"tilt={tilt} coarse={coarse}: image {e_img:.2e}, grad pos {errs[0]:.2e}, phase {errs[1]:.2e}, "
+          f"weight {errs[2]:.2e}")
     assert e_img <= 1e-5
     assert max(errs) <= ADJ_TOL
 

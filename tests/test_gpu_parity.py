@@ -344,6 +344,8 @@ def test_linearity_and_pulse_split(lib):
     assert rel_err(a * x.astype(np.complex128) + b * y, z) <= 1e-5
     z4 = _lattice_split(sc, pulse_split=4).cpu().numpy()
     assert rel_err(x, z4) <= 1e-6
+    z0 = _lattice_split(sc, pulse_split=0).cpu().numpy()  # the split that fills the GPU (64 tiles here: > 1)
+    assert rel_err(x, z0) <= 1e-6
 
 
 def test_resident_graph_replay_bitexact(golden, backend):
