@@ -1196,6 +1196,7 @@ __device__ __noinline__ void lattice_adjoint_slow(const SplitParams& P, const Ti
         px[k].psi = 0.0f;
     }
     const float gre[kPX] = {g0, g1, g2, g3}, gim[kPX] = {h0, h1, h2, h3};
+    static_assert(AdjointBody<true, false>::kRecMode == 0, "the fallback works from per-pixel offsets");
     AdjointBody<true, false> body{P, S, px, gre, gim, red, part, kSplitTilePixels};
     body.slow(c0, nslow, srec);  // writes A directly
 }
