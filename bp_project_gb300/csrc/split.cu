@@ -1290,10 +1290,12 @@ struct LatticeAdjointBody {
                 const float s = qp - (tq - kMagic);
                 const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
                 const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
-                const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
-                const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
-                const float dvr = fmaf(fmaf(3.0f * c23.z, s, 2.0f * c23.x), s, c01.z);
-                const float dvi = fmaf(fmaf(3.0f * c23.w, s, 2.0f * c23.y), s, c01.w);
+                // Horner for the value; the derivative c1 + 2 c2 s + 3 c3 s^2 = p2 + s (p1 + c3 s) reuses
+                // its partial results p1 = c3 s + c2, p2 = p1 s + c1.
+                const float pr1 = fmaf(c23.z, s, c23.x), pi1 = fmaf(c23.w, s, c23.y);
+                const float pr2 = fmaf(pr1, s, c01.z), pi2 = fmaf(pi1, s, c01.w);
+                const float vr = fmaf(pr2, s, c01.x), vi = fmaf(pi2, s, c01.y);
+                const float dvr = fmaf(s, fmaf(c23.z, s, pr1), pr2), dvi = fmaf(s, fmaf(c23.w, s, pi1), pi2);
                 const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
                 float sn, cs;
                 __sincosf(ang, &sn, &cs);
