@@ -1299,13 +1299,15 @@ struct LatticeAdjointBody {
                 const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
                 float sn, cs;
                 __sincosf(ang, &sn, &cs);
+                // h = conj(G) exp(i phi): U += v h, and the position weight
+                // Re(conj(G) (v'/dr + i k v) exp(i phi)) / d = (Re(v' h) / dr - k Im(v h)) / d.
                 const float gr = gre[k], gi = gim[k];
-                const float er = vr * cs - vi * sn, ei = vr * sn + vi * cs;  // v exp(i phi)
-                u0 = fmaf(gr, er, fmaf(gi, ei, u0));
-                u1 = fmaf(gr, ei, fmaf(-gi, er, u1));
-                const float zr = fmaf(dvr, inv_dr, -kr * vi), zi = fmaf(dvi, inv_dr, kr * vr);
-                const float fr = zr * cs - zi * sn, fi = zr * sn + zi * cs;
-                const float tt = fmaf(gr, fr, gi * fi) * rcp_approx(R + L + eps);
+                const float hr = fmaf(gr, cs, gi * sn), hi = fmaf(gr, sn, -gi * cs);
+                u0 = fmaf(vr, hr, fmaf(-vi, hi, u0));
+                const float w1 = fmaf(vr, hi, vi * hr);
+                u1 += w1;
+                const float q = fmaf(dvr, hr, -dvi * hi);
+                const float tt = fmaf(q, inv_dr, -kr * w1) * rcp_approx(R + (L + eps));
                 t0 += tt;
                 s1 = fmaf(kc, tt, s1);
             }
