@@ -348,6 +348,21 @@ def test_linearity_and_pulse_split(lib):
     assert rel_err(x, z0) <= 1e-6
 
 
+@pytest.mark.parametrize("pulses,rows,cols", [(3, 7, 5), (64, 1, 1), (40, 33, 65)])
+def test_auto_pulse_split_small_cases(lib, pulses, rows, cols):
+    """pulse_split=0 picks at most `pulses` splits and matches the unsplit image to FP32 rounding."""
+    from bp_project_gb300 import core
+    sc = _scene("c0", pulses=pulses, image_side=64)
+    lat = sc.lattice
+    args = [_dev(a, dt) for a, dt in ((sc.data, torch.complex64), (sc.position, torch.float64),
+                                      (sc.weight, torch.float64), (sc.phase, torch.float64))]
+    geo = (lat.origin, lat.step_row, lat.step_col, rows, cols, sc.range_start, sc.data_dr, sc.k)
+    one = core.backproject_lattice(*args, *geo, mode="split", pulse_split=1).cpu().numpy()
+    auto = core.backproject_lattice(*args, *geo, mode="split", pulse_split=0).cpu().numpy()
+    assert np.abs(one).max() > 0
+    assert rel_err(one, auto) <= 1e-6
+
+
 def test_resident_graph_replay_bitexact(golden, backend):
     from bp_project_gb300.batched_resident_backend import BatchedResidentProgram
     from bp_project_gb300.resident_backend import ResidentProgram
