@@ -92,15 +92,47 @@ def morton_order(xyz: np.ndarray) -> np.ndarray:
     return np.argsort(spread(q[:, 0]) | (spread(q[:, 1]) << 1), kind="stable")
 
 
+LATTICE_TOL_M = 1e-9  # points within 1 nm of an affine lattice are imaged on it (phase change < 1e-6 rad)
+
+
+def lattice_of(points):
+    """(origin, step_row, step_col, rows, cols) if ``points`` [n, 3] (float64) list an affine lattice
+    origin + i step_row + j step_col in row-major order to within LATTICE_TOL_M, else None."""
+    n = len(points)
+    if n < 2:
+        return None
+    o, sc = points[0], points[1] - points[0]
+    j = np.arange(n, dtype=np.float64)[:, None]
+    off = np.abs(points - (o + j * sc)).max(axis=1) > LATTICE_TOL_M
+    cols = int(np.argmax(off)) if off.any() else n
+    if n % cols:
+        return None
+    rows = n // cols
+    sr = points[cols] - o if rows > 1 else np.zeros(3)
+    i, jj = np.divmod(np.arange(n), cols)
+    if np.abs(points - (o + i[:, None] * sr + jj[:, None] * sc)).max() > LATTICE_TOL_M:
+        return None
+    return tuple(o), tuple(sr), tuple(sc), rows, cols
+
+
 def backproject_points(data, pos, xyz, r_start, dr, k, weight, phase, mode=DEFAULT_MODE):
-    """Direct BP at arbitrary xyz: sum_n w[n] sample1 exp(j(k r + phase[n])) (ffbp.py:43-55)."""
+    """Direct BP at arbitrary xyz: sum_n w[n] sample1 exp(j(k r + phase[n])) (ffbp.py:43-55).
+
+    In split mode a host point list that is an affine lattice in row-major order (the ground
+    meshgrids of run.py) is imaged by the lattice kernel, whose row/column terms make it the
+    fastest path; any other point list goes through the points kernel in Morton order."""
     keep = _on_device(data, xyz)
     d, p, w, ph = _inputs(data, pos, weight, phase)
     order = None
     if isinstance(xyz, torch.Tensor):
         pts = xyz.to(device=d.device, dtype=torch.float64).contiguous()
     else:
-        host = np.ascontiguousarray(xyz, dtype=np.float64)
+        host = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        grid = lattice_of(host) if mode == "split" and len(host) > 1024 else None
+        if grid is not None:
+            origin, sr, sc, rows, cols = grid
+            img = core.backproject_lattice(d, p, w, ph, origin, sr, sc, rows, cols, r_start, dr, k, mode=mode)
+            return _result(img.reshape(-1), keep)
         if mode == "split" and len(host) > 1024:
             order = morton_order(host)
             host = np.ascontiguousarray(host[order])

@@ -208,3 +208,23 @@ def test_decode_iq_validates_on_host(lib):
     assert h.sarbp_decode_iq(None, 4, 1152, 160, 240, fake, None) == lib.SARBP_ERR_TYPE
     assert h.sarbp_decode_iq(fake, 4, 1152, 160, 300, fake, None) == lib.SARBP_ERR_VALUE  # I/Q past the frame
     assert h.sarbp_decode_iq(fake, 4, 1150, 160, 240, fake, None) == lib.SARBP_ERR_TYPE   # misaligned frames
+
+
+def test_lattice_detection_for_point_lists():
+    """ffbp.lattice_of recognises row-major affine lattices (to 1 nm) and rejects anything else."""
+    from bp_project_gb300.ffbp import lattice_of
+    xs = 2645.8 + np.arange(40) * 0.5
+    ys = -12.3 + np.arange(70) * 0.5
+    xx, yy = np.meshgrid(xs, ys, indexing="ij")
+    pts = np.column_stack([xx.ravel(), yy.ravel(), np.zeros(xx.size)])
+    origin, sr, sc, rows, cols = lattice_of(pts)
+    assert (rows, cols) == (40, 70) and np.allclose(sr, (0.5, 0, 0)) and np.allclose(sc, (0, 0.5, 0))
+    assert np.allclose(origin, pts[0])
+    tilted = pts + np.column_stack([np.zeros(len(pts)), np.zeros(len(pts)), 0.01 * np.repeat(np.arange(40), 70)])
+    assert lattice_of(tilted)[3:] == (40, 70)
+    shuffled = pts[np.random.default_rng(0).permutation(len(pts))]
+    assert lattice_of(shuffled) is None
+    nudged = pts.copy()
+    nudged[500, 0] += 1e-6
+    assert lattice_of(nudged) is None
+    assert lattice_of(pts[:1000]) is None  # not whole rows
