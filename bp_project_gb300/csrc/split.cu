@@ -1754,8 +1754,10 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
                 sm = fmaf(rb.x, q.ex, sm);
                 sm = fmaf(rb.y, q.ey, sm);
                 sm = fmaf(rb.z, q.ez, sm);
-                const float tot = (tb - round_magic(tb)) + sm;
-                const float ang = (tot - round_magic(tot)) * kTwoPiF;
+                // The reduced exact term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps (eps is second
+                // order in the pulse's offset from the leaf centre), so the angle stays within a few
+                // turns, which the hardware sin/cos reduce themselves.
+                const float ang = ((tb - round_magic(tb)) + sm) * kTwoPiF;
                 float sn, cs;
                 __sincosf(ang, &sn, &cs);
                 q.ar = fmaf(vr, cs, q.ar);
