@@ -43,7 +43,7 @@ REF_SAMPLE_PIXELS = 131072          # pixels per step of the reference arm (~1 s
 # DRAM bytes (read + write) of one split_lattice_kernel launch on this workload, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum): only the ~920 range bins per pulse that the scene spans
 # are read, so traffic is far below the algorithmic 302 MB.
-NCU_TRAFFIC_BYTES = 31.905536e6 + 3.394304e6
+NCU_TRAFFIC_BYTES = 33.299456e6 + 83.196160e6  # 4 pulse splits: the partial images are written
 L2_FLUSH_BYTES = 256 << 20          # written between timed steps: twice GB300's 129 MB L2
 
 
@@ -357,7 +357,7 @@ def run_batch(args, rank):
         if isinstance(sc, DirectScene) and i < 8:
             default_ref[i] = core.backproject_lattice(sc.data, sc.pos, sc.weight, sc.phase, sc.origin, sc.step_row,
                                                       sc.step_col, sc.rows, sc.cols, sc.range_start, sc.data_dr,
-                                                      sc.k, mode="split")
+                                                      sc.k, mode="split", pulse_split=1)
     autotune.apply(items, choices)
     blocks, block_timings = autotune.tune_blocks(items)
 
@@ -643,7 +643,10 @@ def main():
         "dtype": "f32 (split precision: FP64 per tile-pulse)", "data": "synthetic",
         "config": {"workload": WORKLOAD, "pulses": cfg.pulses, "samples": cfg.samples,
                    "image": [lat.rows, lat.cols], "pixel_spacing_m": cfg.pixel_spacing,
-                   "l2": "L2 flushed between timed steps (256 MB write outside the step's events); 268 MB range data", "parallelism": f"replicas x{world}"},
+                   "l2": "L2 flushed between timed steps (256 MB write outside the step's events); 268 MB range data",
+                   "pulse_split": core.lattice_pulse_split(lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                                           "split"),
+                   "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * units / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                 "path": "every step: pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), "

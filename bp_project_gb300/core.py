@@ -119,12 +119,20 @@ def backproject_points(data, pos, weight, phase, xyz, range_start, data_dr, k, m
     return out
 
 
+def lattice_pulse_split(origin, step_row, step_col, rows, cols, mode=DEFAULT_MODE):
+    """The pulse split backproject_lattice(pulse_split=0) uses for this lattice on the current GPU."""
+    lat = nat.lattice(origin, step_row, step_col, rows, cols)
+    nbytes = nat.load().sarbp_backproject_lattice_workspace(nat.mode_id(mode), ctypes.byref(lat), 0)
+    return max(1, int(nbytes) // (int(rows) * int(cols) * 8))
+
+
 def backproject_lattice(data, pos, weight, phase, origin, step_row, step_col, rows, cols, range_start, data_dr, k,
-                        mode=DEFAULT_MODE, pulse_split=1, out=None):
+                        mode=DEFAULT_MODE, pulse_split=0, out=None):
     """Direct BP on the lattice origin + i*step_row + j*step_col -> complex64 [rows, cols].
 
     pulse_split > 1 splits each tile's pulses over that many CTAs (partial images summed in
-    fixed order); 0 lets the library pick the split that fills the GPU for this lattice."""
+    fixed order); 0 (the default) lets the library pick the split that fills the GPU for this
+    lattice, which also shortens each FP32 partial sum."""
     p, s = check_pulses(data, pos, weight, phase)
     lat = nat.lattice(origin, step_row, step_col, rows, cols)
     if out is None:

@@ -49,7 +49,8 @@ def single(sc):
     from bp_project_gb300.batch import DirectScene
     if isinstance(sc, DirectScene):
         return core.backproject_lattice(sc.data, sc.pos, sc.weight, sc.phase, sc.origin, sc.step_row, sc.step_col,
-                                        sc.rows, sc.cols, sc.range_start, sc.data_dr, sc.k, mode="split")
+                                        sc.rows, sc.cols, sc.range_start, sc.data_dr, sc.k, mode="split",
+                                        pulse_split=1)  # a batch scene sums its pulses in one pass
     prog = core.FFBPProgram(sc.plan.nodes(), sc.plan.crop_r, sc.plan.crop_u, mode="split", device=sc.data.device)
     try:
         return prog.execute(sc.data, sc.pos, sc.weight, sc.phase, sc.range_start, sc.data_dr, sc.k).clone()
