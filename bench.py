@@ -402,6 +402,15 @@ def run_batch(args, rank):
             p.close()
     px = batch.info["pixel_pulses"]
     direct_px = sum(sc.rows * sc.cols * sc.data.shape[0] for sc in items if isinstance(sc, DirectScene))
+    lat_ms = batch.scene_latencies_ms()  # one traced execution, outside the timed replays
+    kinds = ["direct" if isinstance(sc, DirectScene) else "ffbp" for sc in items]
+
+    def spread(v):
+        v = np.sort(np.asarray(v, dtype=np.float64))
+        if not len(v):
+            return None
+        return {"min": float(v[0]), "median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)),
+                "max": float(v[-1])}
     line = {
         "metric": "batched scenes: Gpixel·pulses/s (direct-equivalent) and scenes/s", "value": px / (batch_ms / 1e3) / 1e9,
         "unit": "Gpixel·pulses/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps,
@@ -419,6 +428,11 @@ def run_batch(args, rank):
         "autotune_blocks_per_sm": {"chosen": blocks, "ms": block_timings},
         "autotune_s": tune_s, "synthesis_s": synth_s,
         "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / batch_ms,
+        "scene_latency_ms": {"all": spread(lat_ms),
+                             "direct": spread([t for t, k in zip(lat_ms, kinds) if k == "direct"]),
+                             "ffbp": spread([t for t, k in zip(lat_ms, kinds) if k == "ffbp"]),
+                             "how": "completion of each scene's last work item from the batch's start (GPU "
+                                    "nanosecond timer), one traced execution"},
         "tuned_vs_default_shape_err_max": max(errs) if errs else None,
         "workspace_gb": batch.workspace_bytes / 1e9,
         "clocks": clocks.summary(),

@@ -99,6 +99,7 @@ SIGNATURES = {
                           ctypes.POINTER(_D)], _I),
     "sarbp_batch_bind": ([_P, _P, _Z, _P], _I),
     "sarbp_batch_execute": ([_P, _P], _I),
+    "sarbp_batch_set_trace": ([_P, _P], _I),
     "sarbp_rc_prepare": ([_P, _I, _I, _I, _P, _P], _I),
     "sarbp_decode_iq": ([_P, _I, _I64, _I, _I, _P, _P], _I),
     "sarbp_rc_filter": ([_P, _P, _I, _I, _I, _P, _P], _I),

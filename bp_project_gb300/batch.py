@@ -120,6 +120,20 @@ class SceneBatch:
             raise RuntimeError("batch is closed")
         nat.check(nat.load().sarbp_batch_execute(self._handle, core.stream_handle()), "batch_execute")
 
+    def scene_latencies_ms(self):
+        """Per-scene completion times (ms from the batch's start) of one traced execution: each
+        work item raises its scene's slot to the GPU's nanosecond timer when it finishes."""
+        lib = nat.load()
+        trace = torch.zeros(len(self.scenes) + 1, dtype=torch.int64, device=self.workspace.device)
+        nat.check(lib.sarbp_batch_set_trace(self._handle, core._ptr(trace)), "batch_set_trace")
+        try:
+            self.execute()
+            torch.cuda.synchronize(self.workspace.device)
+        finally:
+            nat.check(lib.sarbp_batch_set_trace(self._handle, None), "batch_set_trace")
+        t = trace.cpu().numpy()
+        return (t[:-1] - t[-1]) / 1e6
+
     def capture_graph(self):
         """Capture one execute into a CUDA graph (warm once first, so the capture sees no first-use work)."""
         self.execute()

@@ -41,6 +41,7 @@ struct sarbp_batch {
     size_t scene_off = 0, node_off = 0, bp_off = 0, merge_off = 0, leaf_off = 0, counter_off = 0, table_off = 0,
            prec_off = 0, crec_off = 0, arena_off = 0, total = 0;
     void* bound = nullptr;
+    unsigned long long* trace = nullptr;  // per-scene completion times (ns) + the start time, or none
     int launches = 0;
 };
 
@@ -262,6 +263,12 @@ size_t sarbp_batch_workspace_bytes(const sarbp_batch* batch) { return batch ? ba
 
 int sarbp_batch_launch_count(const sarbp_batch* batch) { return batch ? batch->launches : 0; }
 
+int sarbp_batch_set_trace(sarbp_batch* batch, unsigned long long* trace) {
+    if (!batch) return fail(SARBP_ERR_TYPE, "batch must not be NULL");
+    batch->trace = trace;
+    return SARBP_OK;
+}
+
 int sarbp_batch_info(const sarbp_batch* batch, int* bp_items, int* merge_items, int* max_height, int* bp_blocks,
                      double* pixel_pulses) {
     if (!batch) return fail(SARBP_ERR_TYPE, "batch must not be NULL");
@@ -316,8 +323,10 @@ int sarbp_batch_execute(const sarbp_batch* batch, void* stream) {
     char* crecs = base + batch->crec_off;
     float2* arena = reinterpret_cast<float2*>(base + batch->arena_off);
     cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(int) * (2 + batch->max_height), s);
+    unsigned long long* trace = batch->trace;
+    if (trace && e == cudaSuccess) e = cudaMemsetAsync(trace, 0, sizeof(unsigned long long) * batch->n_scenes, s);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "batch counters: %s", cudaGetErrorString(e));
-    int st = SARBP_OK;
+    int st = trace ? launch_split_batch_trace_start(trace + batch->n_scenes, s) : SARBP_OK;
     if (batch->ffbp_scenes)
         st = launch_split_batch_prologue(scenes, nodes, (int)batch->nodes.size(), batch->max_dim, leaves,
                                          (int)batch->leaves.size(), merge_items, (int)batch->merge_items.size(),
@@ -325,16 +334,16 @@ int sarbp_batch_execute(const sarbp_batch* batch, void* stream) {
     const int n_leaf = (int)batch->bp_items.size() - batch->n_direct;
     if (st == SARBP_OK)
         st = launch_split_batch_direct(scenes, bp_items, batch->n_direct, counters, batch->bp_blocks,
-                                       batch->direct_smem, s);
+                                       batch->direct_smem, trace, s);
     if (st == SARBP_OK)
         st = launch_split_batch_leaves(scenes, nodes, bp_items + batch->n_direct, n_leaf, tables, precs, arena,
-                                       counters + 1, batch->leaf_blocks, batch->leaf_smem, s);
+                                       counters + 1, batch->leaf_blocks, batch->leaf_smem, trace, s);
     const size_t crec_size = split_ffbp_child_record_bytes();
     for (int h = 1; h <= batch->max_height && st == SARBP_OK; ++h) {
         const int first = batch->level_begin[h - 1], count = batch->level_count[h - 1];
         st = launch_split_batch_merges(scenes, nodes, merge_items + first, count, tables,
                                        crecs + 2 * (size_t)first * crec_size, arena, counters + 1 + h,
-                                       std::min(batch->merge_blocks, std::max(1, count)), s);
+                                       std::min(batch->merge_blocks, std::max(1, count)), trace, s);
     }
     return st;
 }

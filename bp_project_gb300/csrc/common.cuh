@@ -200,14 +200,15 @@ int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_
 int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int n_nodes, int max_dim,
                                 const int* leaves, int n_leaves, const TileItem* merge_items, int n_merge_items,
                                 float4* tables, void* precs, void* crecs, float2* arena, cudaStream_t s);
+int launch_split_batch_trace_start(unsigned long long* t0, cudaStream_t s);
 int launch_split_batch_direct(const void* scenes, const TileItem* items, int nitems, int* counter, int blocks,
-                              size_t smem, cudaStream_t s);
+                              size_t smem, unsigned long long* trace, cudaStream_t s);
 int launch_split_batch_leaves(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
                               const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
-                              size_t smem, cudaStream_t s);
+                              size_t smem, unsigned long long* trace, cudaStream_t s);
 int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
                               const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
-                              cudaStream_t s);
+                              unsigned long long* trace, cudaStream_t s);
 
 // Polar image -> flat ground lattice, split precision (evaluate_image on lattice points).
 int launch_split_evaluate_lattice(const float2* image, const PolarDesc& grid, const sarbp_lattice& lattice, double k,

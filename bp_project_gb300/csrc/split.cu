@@ -2304,6 +2304,24 @@ struct BatchScene {
     long long prec_offset;  // FFBP: first pulse record of the scene
 };
 
+// Completion time of an item for the scene's trace slot (max over the scene's items): the
+// GPU's nanosecond global timer, after every thread of the block is done with the item.
+__device__ __forceinline__ void trace_item(unsigned long long* trace, int scene) {
+    if (!trace) return;  // uniform
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        atomicMax(trace + scene, t);
+    }
+}
+
+__global__ void batch_trace_start_kernel(unsigned long long* t0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *t0 = t;
+}
+
 __device__ __forceinline__ int next_item(int* counter, int& s_item) {
     __syncthreads();  // every thread is done with the previous item's shared state
     if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
@@ -2321,7 +2339,7 @@ __device__ __forceinline__ void load_scene(const BatchScene* __restrict__ scenes
 // Direct tiles of every direct scene (flat lattices only, checked when the batch is created).
 __global__ void __launch_bounds__(kThreads, 4) batch_direct_kernel(const BatchScene* __restrict__ scenes,
                                                                    const TileItem* __restrict__ items, int nitems,
-                                                                   int* counter) {
+                                                                   int* counter, unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     __shared__ int s_item, s_scene;
@@ -2336,6 +2354,7 @@ __global__ void __launch_bounds__(kThreads, 4) batch_direct_kernel(const BatchSc
             if (threadIdx.x == 0) s_scene = it.pad;
         }
         lattice_tile(sc.P, sc.lat, sc.lc, it.tile_r, it.tile_u, 0, sc.P.in.pulses, sc.P.out, S, smem);
+        trace_item(trace, it.pad);
     }
 }
 
@@ -2345,7 +2364,8 @@ __global__ void __launch_bounds__(kThreads, 3) batch_leaf_kernel(const BatchScen
                                                                  const TileItem* __restrict__ items, int nitems,
                                                                  const float4* __restrict__ tables,
                                                                  const PulseRec* __restrict__ precs,
-                                                                 float2* __restrict__ arena, int* counter) {
+                                                                 float2* __restrict__ arena, int* counter,
+                                                                 unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
     __shared__ int s_base[kMaxLeafChunk];
     __shared__ float s_wt[kMaxLeafChunk];
@@ -2361,6 +2381,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_leaf_kernel(const BatchScen
             if (threadIdx.x == 0) s_scene = it.pad;
         }
         leaf_tile(sc.P, nodes, it, tables, precs + sc.prec_offset, arena, nullptr, -1, smem, s_base, s_wt, s_nfit);
+        trace_item(trace, it.pad);
     }
 }
 
@@ -2369,7 +2390,8 @@ __global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchSce
                                                                   const TileItem* __restrict__ items, int nitems,
                                                                   const float4* __restrict__ tables,
                                                                   const ChildRec* __restrict__ crecs,
-                                                                  float2* __restrict__ arena, int* counter) {
+                                                                  float2* __restrict__ arena, int* counter,
+                                                                  unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
     __shared__ ChildRec C[2];
@@ -2379,6 +2401,7 @@ __global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchSce
         if (idx >= nitems) return;
         const TileItem it = items[idx];
         merge_tile(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, nullptr, -1, S, smem);
+        trace_item(trace, it.pad);
     }
 }
 
@@ -2465,36 +2488,43 @@ int launch_split_batch_prologue(const void* scenes, const PolarDesc* nodes, int 
     return SARBP_OK;
 }
 
+int launch_split_batch_trace_start(unsigned long long* t0, cudaStream_t s) {
+    batch_trace_start_kernel<<<1, 1, 0, s>>>(t0);
+    note_launches(1);
+    return check_launch("batch_trace_start");
+}
+
 int launch_split_batch_direct(const void* scenes, const TileItem* items, int nitems, int* counter, int blocks,
-                              size_t smem, cudaStream_t s) {
+                              size_t smem, unsigned long long* trace, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     if (int st = prepare(batch_direct_kernel, smem)) return st;
     batch_direct_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), items, nitems,
-                                                       counter);
+                                                       counter, trace);
     note_launches(1);
     return check_launch("batch_direct");
 }
 
 int launch_split_batch_leaves(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
                               const float4* tables, const void* precs, float2* arena, int* counter, int blocks,
-                              size_t smem, cudaStream_t s) {
+                              size_t smem, unsigned long long* trace, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     if (int st = prepare(batch_leaf_kernel, smem)) return st;
     batch_leaf_kernel<<<blocks, kThreads, smem, s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes, items, nitems,
-                                                     tables, reinterpret_cast<const PulseRec*>(precs), arena, counter);
+                                                     tables, reinterpret_cast<const PulseRec*>(precs), arena, counter,
+                                                     trace);
     note_launches(1);
     return check_launch("batch_leaves");
 }
 
 int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const TileItem* items, int nitems,
                               const float4* tables, const void* crecs, float2* arena, int* counter, int blocks,
-                              cudaStream_t s) {
+                              unsigned long long* trace, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     if (int st = prepare(batch_merge_kernel, merge_smem())) return st;
     batch_merge_kernel<<<blocks, kThreads, merge_smem(), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
                                                               items, nitems, tables,
                                                               reinterpret_cast<const ChildRec*>(crecs), arena,
-                                                              counter);
+                                                              counter, trace);
     note_launches(1);
     return check_launch("batch_merges");
 }

@@ -229,6 +229,12 @@ int sarbp_batch_info(const sarbp_batch* batch, int* bp_items, int* merge_items, 
 /* Uploads the scene, node and work tables into workspace (256-byte aligned); synchronises `stream`. */
 int sarbp_batch_bind(sarbp_batch* batch, void* workspace, size_t workspace_bytes, void* stream);
 int sarbp_batch_execute(const sarbp_batch* batch, void* stream);
+/* Per-scene completion tracing for the following executes: trace is a device array of
+ * n_scenes + 1 uint64; execute zeroes the first n_scenes, writes the GPU's nanosecond timer at its
+ * start into trace[n_scenes] and, as each work item finishes, raises trace[scene] to the timer, so
+ * trace[i] - trace[n_scenes] is scene i's latency within the batch.  NULL switches tracing off (a
+ * captured graph keeps the setting it was captured with). */
+int sarbp_batch_set_trace(sarbp_batch* batch, unsigned long long* trace);
 
 /* ---- range compression (sar_io.range_compress, sar_io.py:116-139) --------- */
 

@@ -94,6 +94,28 @@ def test_batch_equals_single_scene_paths(small_batch):
     batch.close()
 
 
+def test_batch_scene_latency_trace(small_batch):
+    """A traced execution reports every scene's completion after the batch's start, within the batch's own
+    duration, and leaves the images unchanged; FFBP scenes finish with their root merge."""
+    from bp_project_gb300.batch import SceneBatch
+    batch = SceneBatch(small_batch)
+    batch.execute()
+    torch.cuda.synchronize()
+    first = [o.clone() for o in batch.outputs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    lat = batch.scene_latencies_ms()
+    e1.record()
+    torch.cuda.synchronize()
+    total = e0.elapsed_time(e1)
+    print("scene latencies (ms):", np.round(lat, 3), "batch", round(total, 3))
+    assert len(lat) == len(small_batch)
+    assert np.all(lat > 0) and np.all(lat <= total * 1.05 + 0.05)
+    for a, b in zip(first, batch.outputs):
+        assert torch.equal(a, b)
+    batch.close()
+
+
 def test_batch_tile_shapes_and_chunks(small_batch):
     """Other tile shapes / chunks stay within split precision of the default; chunks alone change nothing."""
     from bp_project_gb300.batch import DirectScene, SceneBatch
