@@ -2,12 +2,13 @@
 //
 // Work unit: one CTA = one tile of 1024 output pixels (256 threads x 4 pixels),
 // looping over its pulses in shared-memory chunks.  Precision plan (per pixel p,
-// pulse n, tile centre c, all FP64 work is per tile or per (tile, pulse)):
+// pulse n, tile centre c; the wide-precision work is per tile or per (tile, pulse), in
+// two-float FP32 from the FP64 inputs split once into hi + lo):
 //
-//   d(p,n) = R + L + eps,    R = |c - pos_n| (FP64, per tile-pulse)
+//   d(p,n) = R + L + eps,    R = |c - pos_n| (two-float, per tile-pulse)
 //                            L = u . delta_p  (u = (c - pos_n)/R, delta_p = p - c)
 //                            eps = |delta_p x u|^2 / (R + L + d)   (<= ~1 cm, FP32)
-//   phase turns = frac(K R + phase_n / 2pi)            FP64 -> FP32, per tile-pulse
+//   phase turns = frac(K R + phase_n / 2pi)            two-float -> FP32, per tile-pulse
 //               + frac(K u . delta_p)                  exact: W_hi . delta_hi
 //               + W_hi . delta_lo + W_lo . delta_p     FP32, tiny terms
 //               + K eps - K r_p (polar demodulation, per pixel)
@@ -29,8 +30,8 @@
 // Lagrange cubic (weight folded in), 32 bytes per bin; a pixel-pulse is then
 // two 16-byte shared loads and six FMAs.  Bins whose taps leave the row are
 // stored as zero, which reproduces the reference's support rule
-// (fast_bp/ffbp.py:27).  A tile whose window would not fit the staged bins
-// runs a chunk through an FP64 per-sample fallback instead.
+// (fast_bp/ffbp.py:27).  A pulse whose window would not fit the staged bins, or that lies
+// outside the precision envelope, runs through a two-float per-sample fallback instead.
 #include <limits.h>
 #include <math.h>
 
@@ -284,7 +285,7 @@ __device__ void setup_polar(const SplitParams& P, const Job& J, TileShared& S, P
     __syncthreads();  // the tables alias the window region
 }
 
-// Polar tile set-up from per-node FP64 tables stored as float pairs (FFBP):
+// Polar tile set-up from per-node tables of float pairs (FFBP):
 // FP32 two-float arithmetic only, no block reductions.  Row i holds three
 // float4: (g hi, g lo, psi, 0), (g/r hi, g/r lo, -oz/r hi, -oz/r lo) and
 // (2r, frac(Q) - 1/2, floor(Q) bits, 0) with g = sqrt(r^2 - oz^2),
@@ -573,9 +574,6 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
     }
 }
 
-// FP64 per-sample evaluation of one pixel over pulses [c0, c0 + chn): the
-// fallback for a pulse whose range window does not fit the staged bins.
-// Everything is passed by value so the caller's pixel state stays in registers.
 // ---- two-float arithmetic (unevaluated sums hi + lo of two FP32 numbers) ----------------
 //
 // Error-free transformations (Knuth's two-sum, the FMA form of Dekker's product) give about
@@ -705,8 +703,6 @@ __device__ __forceinline__ bool slow_sample(const SplitParams& P, const SlowRec&
 }
 
 
-// Per (tile, pulse) record in FP64, computed by lane `lane` of warp 0.  Returns
-// the number of window entries the pulse needs (cap + 1 if it cannot be staged).
 // Two-float record of a pulse the fast path cannot stage (out of line: it is rare, and its
 // FP64 temporaries would otherwise add to the registers of every chunk kernel).
 __device__ __noinline__ void slow_record(const SplitParams& P, const TileShared& S, int n, SlowRec* out) {
@@ -840,7 +836,7 @@ __device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* s
 }
 
 // Chunk driver shared by the forward and adjoint kernels: per chunk of up to 64
-// pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, FP64,
+// pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, two-float,
 // on two SM sub-partitions at once) and pack the pulses' range windows, all warps
 // stage the windows (Horner coefficients, times the pulse weight when `weighted`),
 // then `body.fast(rec, win, nfit, c0)` consumes them; a pulse whose window cannot be
