@@ -110,7 +110,7 @@ PulseInputs inputs_of(const float* data, int pulses, int samples, const double* 
 }
 
 
-// Envelope assumed for point tiles: tiles wider than this run through the FP64 fallback.
+// Window radius assumed for point tiles: pulses of wider tiles run through the two-float fallback.
 constexpr double kPointRadius = 24.0;
 
 }  // namespace

@@ -32,11 +32,12 @@
  *   SARBP_FP64  FP64 geometry, interpolation, phase and accumulation
  *   SARBP_FP32  FP32 everything (the reference's fp32 policy)
  *   SARBP_MIXED FP64 geometry and phase, FP32 interpolation and accumulation
- *   SARBP_SPLIT FP32 arithmetic with FP64 only per (pixel tile, pulse) and per
- *               tile: tile-centre ranges in FP64, per-pixel range offsets as
- *               exact split products, phase reduced in turns before a hardware
- *               sin/cos.  Relative error vs FP64 is ~1e-6 (stated per image
- *               by the tests); this is the fast path.
+ *   SARBP_SPLIT FP32 arithmetic with wide precision only per (pixel tile, pulse)
+ *               and per tile: tile-centre ranges in two-float FP32 (~44 bits)
+ *               from the FP64 inputs, per-pixel range offsets as exact split
+ *               products, phase reduced in turns before a hardware sin/cos.
+ *               Relative error vs FP64 is ~1e-6 (stated per image by the
+ *               tests); this is the fast path.
  * The first three follow the reference's MODES (fast_bp/gpu_backend.py:57,
  * gpu/kernels.cu:1-6).
  */
@@ -324,7 +325,7 @@ int sarbp_evaluate_image(const float* image, const sarbp_polar_grid* grid, const
                          double k, float* out, void* stream);
 
 /* evaluate_image on the points of a ground lattice (z components ignored), out
- * complex64 [rows, cols], in split precision: FP64 once per 32 x 32 pixel tile,
+ * complex64 [rows, cols], in split precision: two-float once per 32 x 32 pixel tile,
  * FP32 per pixel (offsets as exact split products, phase reduced in turns).
  * Same result as sarbp_evaluate_image on lattice points within ~1e-6 relative;
  * run.py's ground image (run.py:120-125) is this call on its lattice. */
