@@ -150,6 +150,49 @@ __global__ void rc_filter_kernel(const float2* spec, const float2* __restrict__ 
     }
 }
 
+// Row-per-blockIdx.y forms of the filter and the crop: column index from the x grid, no 64-bit
+// division per element (grids with up to 65535 rows).
+__global__ void rc_filter_rows_kernel(const float2* spec, const float2* __restrict__ response, int nfft, int length,
+                                      float2* out) {
+    const int p = blockIdx.y;
+    const int half = nfft / 2, nyq = nfft / 2 + 1;
+    const float2* s = spec + (size_t)p * nfft;
+    float2* o = out + (size_t)p * length;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < length; m += gridDim.x * blockDim.x) {
+        float2 v = make_float2(0.0f, 0.0f);
+        if (length == nfft) {
+            v = cmul(s[m], response[m]);
+        } else if (m < nyq) {
+            v = cmul(s[m], response[m]);
+            if ((nfft & 1) == 0 && m == half) v = make_float2(0.5f * v.x, 0.5f * v.y);
+        } else if (m >= length - (nfft - nyq)) {
+            const int k = m - length + nfft;  // negative frequency bin of the short spectrum
+            v = cmul(s[k], response[k]);
+        } else if ((nfft & 1) == 0 && m == length - half) {
+            v = cmul(s[half], response[half]);
+            v = make_float2(0.5f * v.x, 0.5f * v.y);
+        }
+        o[m] = v;
+    }
+}
+
+__global__ void rc_crop_rows_kernel(const float2* __restrict__ corr, int length, int offset, int samples, float scale,
+                                    float2* __restrict__ out) {
+    const int p = blockIdx.y;
+    const float2* c = corr + (size_t)p * length + offset;
+    float2* o = out + (size_t)p * samples;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < samples; j += gridDim.x * blockDim.x) {
+        const float2 v = c[j];
+        o[j] = make_float2(v.x * scale, v.y * scale);
+    }
+}
+
+// Columns per block of the row kernels: enough blocks for every SM, a few columns per thread.
+dim3 row_grid(int rows, int cols) {
+    int bx = (cols + 4 * kRowThreads - 1) / (4 * kRowThreads);
+    return dim3(bx > 0 ? bx : 1, rows);
+}
+
 __global__ void rc_crop_kernel(const float2* __restrict__ corr, int pulses, int length, int offset, int samples,
                                float scale, float2* __restrict__ out) {
     const long long total = (long long)pulses * samples;
@@ -171,6 +214,17 @@ __global__ void decode_iq_kernel(const unsigned char* __restrict__ frames, int n
         const long long i = t / nr, j = t - i * nr;
         const short2 v = *reinterpret_cast<const short2*>(frames + i * frame_size + iq_offset + 4 * j);
         out[t] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+__global__ void decode_iq_rows_kernel(const unsigned char* __restrict__ frames, long long frame_size, int iq_offset,
+                                      int nr, float2* __restrict__ out) {
+    const long long i = blockIdx.y;
+    const unsigned char* f = frames + i * frame_size + iq_offset;
+    float2* o = out + i * nr;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nr; j += gridDim.x * blockDim.x) {
+        const short2 v = *reinterpret_cast<const short2*>(f + 4 * (long long)j);
+        o[j] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -200,23 +254,34 @@ int launch_rc_prepare(const float2* raw, int pulses, int samples, int nfft, floa
 
 int launch_rc_filter(const float2* spec, const float2* response, int pulses, int nfft, int length, float2* out,
                      cudaStream_t s) {
-    rc_filter_kernel<<<stream_grid((long long)pulses * length), kRowThreads, 0, s>>>(spec, response, pulses, nfft,
-                                                                                    length, out);
+    if (pulses <= 65535)
+        rc_filter_rows_kernel<<<row_grid(pulses, length), kRowThreads, 0, s>>>(spec, response, nfft, length, out);
+    else
+        rc_filter_kernel<<<stream_grid((long long)pulses * length), kRowThreads, 0, s>>>(spec, response, pulses, nfft,
+                                                                                        length, out);
     note_launches(1);
     return check_launch("rc_filter");
 }
 
 int launch_decode_iq(const unsigned char* frames, int n, long long frame_size, int iq_offset, int nr, float2* out,
                      cudaStream_t s) {
-    decode_iq_kernel<<<stream_grid((long long)n * nr), kRowThreads, 0, s>>>(frames, n, frame_size, iq_offset, nr, out);
+    if (n <= 65535)
+        decode_iq_rows_kernel<<<row_grid(n, nr), kRowThreads, 0, s>>>(frames, frame_size, iq_offset, nr, out);
+    else
+        decode_iq_kernel<<<stream_grid((long long)n * nr), kRowThreads, 0, s>>>(frames, n, frame_size, iq_offset, nr,
+                                                                               out);
     note_launches(1);
     return check_launch("decode_iq");
 }
 
 int launch_rc_crop(const float2* corr, int pulses, int length, int offset, int samples, float scale, float2* out,
                    cudaStream_t s) {
-    rc_crop_kernel<<<stream_grid((long long)pulses * samples), kRowThreads, 0, s>>>(corr, pulses, length, offset,
-                                                                                   samples, scale, out);
+    if (pulses <= 65535)
+        rc_crop_rows_kernel<<<row_grid(pulses, samples), kRowThreads, 0, s>>>(corr, length, offset, samples, scale,
+                                                                               out);
+    else
+        rc_crop_kernel<<<stream_grid((long long)pulses * samples), kRowThreads, 0, s>>>(corr, pulses, length, offset,
+                                                                                       samples, scale, out);
     note_launches(1);
     return check_launch("rc_crop");
 }
