@@ -104,6 +104,7 @@ SIGNATURES = {
     "sarbp_decode_iq": ([_P, _I, _I64, _I, _I, _P, _P], _I),
     "sarbp_rc_filter": ([_P, _P, _I, _I, _I, _P, _P], _I),
     "sarbp_rc_crop": ([_P, _I, _I, _I, _I, ctypes.c_float, _P, _P], _I),
+    "sarbp_tile_argmax": ([_P, _I, _I, _I, _I, _P, _P, _P], _I),
     "sarbp_sosfiltfilt_workspace": ([_I, _I, _I], _Z),
     "sarbp_sosfiltfilt": ([_P, _I, _I, _P, _P, _I, _P, _I, _P, _P, _Z, _P], _I),
     "sarbp_regrid": ([_P, ctypes.POINTER(PolarGrid), ctypes.POINTER(PolarGrid), _D, _I, _P, _P], _I),

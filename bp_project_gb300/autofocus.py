@@ -17,6 +17,7 @@ Two estimators of per-pulse navigation errors, both device-resident:
 from __future__ import annotations
 
 import ctypes
+import functools
 import math
 import time
 from dataclasses import dataclass, field
@@ -43,8 +44,10 @@ class SmoothingFilter:
     padlen: int
 
 
+@functools.lru_cache(maxsize=64)
 def butter_lowpass(cutoff, fs, order=4) -> SmoothingFilter:
-    """butter(order, cutoff, fs=fs, output='sos') with sosfiltfilt's default padding (autofocus.py:38)."""
+    """butter(order, cutoff, fs=fs, output='sos') with sosfiltfilt's default padding (autofocus.py:38).
+    Cached per (cutoff, fs, order): the autofocus loop asks for the same few filters every pass."""
     sos = np.ascontiguousarray(signal.butter(order, cutoff, fs=fs, output="sos"), np.float64)
     zi = np.ascontiguousarray(signal.sosfilt_zi(sos), np.float64)
     ntaps = 2 * len(sos) + 1
@@ -125,7 +128,8 @@ def savgol_smooth(x: torch.Tensor, window: int, polyorder: int) -> torch.Tensor:
 # ---- phase-gradient autofocus (fast_bp/autofocus.py) -----------------------------------
 
 def pick_targets(result, nr_tiles=12, nu_tiles=12):
-    """Brightest cell of each of nr_tiles x nu_tiles image tiles (autofocus.py:19-34).
+    """Brightest cell of each of nr_tiles x nu_tiles image tiles (autofocus.py:19-34), one block per
+    tile on the GPU (``sarbp_tile_argmax``).
 
     ``result`` is a ``PolarImage`` whose image is a CUDA tensor.  Returns
     (points float64 [T, 3], powers float64 [T]) on the image's device, cells
@@ -137,15 +141,12 @@ def pick_targets(result, nr_tiles=12, nu_tiles=12):
     if nr < nr_tiles or nu < nu_tiles:
         raise ValueError("the image has fewer rows or columns than tiles")
     dev = image.device
-    a = image.abs().reshape(-1)
-    row_tile = np.repeat(np.arange(nr_tiles), [len(s) for s in np.array_split(np.arange(nr), nr_tiles)])
-    col_tile = np.repeat(np.arange(nu_tiles), [len(s) for s in np.array_split(np.arange(nu), nu_tiles)])
-    ids = torch.from_numpy((row_tile[:, None] * nu_tiles + col_tile[None, :]).reshape(-1)).to(dev)
+    a = image.abs().contiguous()  # float32 [nr, nu], numpy's complex64 magnitude
     ntiles = nr_tiles * nu_tiles
-    tmax = torch.full((ntiles,), -1.0, dtype=a.dtype, device=dev).scatter_reduce(0, ids, a, "amax")
-    flat = torch.arange(a.numel(), device=dev)
-    cand = torch.where(a == tmax[ids], flat, torch.full_like(flat, a.numel()))
-    first = torch.full((ntiles,), a.numel(), dtype=flat.dtype, device=dev).scatter_reduce(0, ids, cand, "amin")
+    tmax = torch.empty(ntiles, dtype=torch.float32, device=dev)
+    first = torch.empty(ntiles, dtype=torch.int64, device=dev)
+    nat.check(nat.load().sarbp_tile_argmax(core._ptr(a), nr, nu, nr_tiles, nu_tiles, core._ptr(tmax), core._ptr(first),
+                                           core.stream_handle()), "tile_argmax")
     ir, iu = first // nu, first % nu
     r = result.r0 + result.dr * ir.double()
     u = result.u0 + result.du * iu.double()

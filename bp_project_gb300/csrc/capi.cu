@@ -361,6 +361,15 @@ int sarbp_sosfiltfilt(const float* x, int rows, int n, const double* sos, const 
                               (cudaStream_t)stream);
 }
 
+int sarbp_tile_argmax(const float* magnitude, int nr, int nu, int nr_tiles, int nu_tiles, float* tile_max,
+                      long long* tile_index, void* stream) {
+    if (!magnitude || !tile_max || !tile_index) return fail(SARBP_ERR_TYPE, "magnitude, tile_max and tile_index must be device pointers");
+    if (nr_tiles < 1 || nu_tiles < 1) return fail(SARBP_ERR_VALUE, "at least one tile per axis is required");
+    if (nr < nr_tiles || nu < nu_tiles) return fail(SARBP_ERR_VALUE, "the image has fewer rows or columns than tiles");
+    if ((long long)nr_tiles * nu_tiles > INT32_MAX) return fail(SARBP_ERR_VALUE, "too many tiles");
+    return launch_tile_argmax(magnitude, nr, nu, nr_tiles, nu_tiles, tile_max, tile_index, (cudaStream_t)stream);
+}
+
 // ---- FFBP building blocks ---------------------------------------------------------------
 int sarbp_regrid(const float* image, const sarbp_polar_grid* src, const sarbp_polar_grid* dst, double k, int mode,
                  float* out, void* stream) {

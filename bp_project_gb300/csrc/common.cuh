@@ -225,6 +225,8 @@ int launch_decode_iq(const unsigned char* frames, int n, long long frame_size, i
 
 // Zero-phase IIR smoothing along rows (autofocus phase-history filter).
 size_t sosfiltfilt_workspace(int rows, int n, int padlen);
+int launch_tile_argmax(const float* a, int nr, int nu, int nr_tiles, int nu_tiles, float* tmax, long long* first,
+                       cudaStream_t s);
 int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const double* zi, int sections, int padlen,
                        double* y, double* ws, cudaStream_t s);
 

@@ -164,7 +164,66 @@ __global__ void __launch_bounds__(32) sosfiltfilt_row_kernel(const float* __rest
     }
 }
 
+// np.array_split bounds: part t of n items over k parts starts at t (n / k) + min(t, n % k).
+__device__ __forceinline__ int split_start(int n, int k, int t) { return t * (n / k) + min(t, n % k); }
+
+// Brightest cell of each tile of an nr x nu image of magnitudes (the autofocus target picks):
+// one block per tile; ties go to the smallest row-major index, as numpy's argmax over the tile.
+constexpr int kArgmaxThreads = 256;
+
+__global__ void __launch_bounds__(kArgmaxThreads) tile_argmax_kernel(const float* __restrict__ a, int nr, int nu,
+                                                                     int nr_tiles, int nu_tiles, float* tmax,
+                                                                     long long* first) {
+    const int tr = blockIdx.x / nu_tiles, tc = blockIdx.x - tr * nu_tiles;
+    const int r0 = split_start(nr, nr_tiles, tr), r1 = split_start(nr, nr_tiles, tr + 1);
+    const int c0 = split_start(nu, nu_tiles, tc), c1 = split_start(nu, nu_tiles, tc + 1);
+    const int w = c1 - c0, cells = (r1 - r0) * w;
+    float best = -1.0f;
+    long long at = (long long)nr * nu;
+    for (int q = threadIdx.x; q < cells; q += kArgmaxThreads) {  // increasing row-major order per thread
+        const int r = r0 + q / w, c = c0 + q - (q / w) * w;
+        const long long idx = (long long)r * nu + c;
+        const float v = a[idx];
+        if (v > best) {
+            best = v;
+            at = idx;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float bv = __shfl_xor_sync(0xffffffffu, best, o);
+        const long long ba = __shfl_xor_sync(0xffffffffu, at, o);
+        if (bv > best || (bv == best && ba < at)) {
+            best = bv;
+            at = ba;
+        }
+    }
+    __shared__ float sv[kArgmaxThreads / 32];
+    __shared__ long long sa[kArgmaxThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sv[warp] = best;
+        sa[warp] = at;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < kArgmaxThreads / 32; ++i)
+            if (sv[i] > best || (sv[i] == best && sa[i] < at)) {
+                best = sv[i];
+                at = sa[i];
+            }
+        tmax[blockIdx.x] = best;
+        first[blockIdx.x] = at;
+    }
+}
+
 }  // namespace
+
+int launch_tile_argmax(const float* a, int nr, int nu, int nr_tiles, int nu_tiles, float* tmax, long long* first,
+                       cudaStream_t s) {
+    tile_argmax_kernel<<<nr_tiles * nu_tiles, kArgmaxThreads, 0, s>>>(a, nr, nu, nr_tiles, nu_tiles, tmax, first);
+    note_launches(1);
+    return check_launch("tile_argmax");
+}
 
 size_t sosfiltfilt_workspace(int rows, int n, int padlen) {
     return (size_t)(n + 2 * padlen) * (size_t)rows * 2 * sizeof(double);

@@ -278,6 +278,14 @@ int sarbp_sosfiltfilt(const float* x, int rows, int n, const double* sos, const 
                       const double* sos_host, int padlen, double* y, void* workspace, size_t workspace_bytes,
                       void* stream);
 
+/* Brightest cell of every tile of a magnitude image (float32 [nr, nu]) split into
+ * nr_tiles x nu_tiles tiles as numpy.array_split does: tile_max float32 and
+ * tile_index int64 (row-major flat index; ties to the smallest) per tile,
+ * tiles in row-major order.  The target picks of the autofocus
+ * (fast_bp/autofocus.py:19-34, per-tile np.argmax). */
+int sarbp_tile_argmax(const float* magnitude, int nr, int nu, int nr_tiles, int nu_tiles, float* tile_max,
+                      long long* tile_index, void* stream);
+
 /* ---- FFBP building blocks (eager schedule) -------------------------------- */
 
 /* Child polar image -> parent polar grid with 4x4 Lagrange and exp(j k (rr-r)).

@@ -108,3 +108,31 @@ def test_entropy_autofocus_refocuses_injected_errors(lib):
           f"after {res.evaluations} evaluations, {res.history[-1][0]:.2f} s")
     assert start > truth + 0.5
     assert res.entropy < truth * 1.01
+
+
+@pytest.mark.parametrize("shape,tiles", [((37, 53), (7, 5)), ((64, 64), (12, 12)), ((300, 211), (12, 12))])
+def test_tile_argmax_matches_numpy(lib, shape, tiles):
+    """sarbp_tile_argmax: numpy.array_split tiles, per-tile np.argmax (first index of the maximum), also on
+    an image whose tiles are constant (every cell ties)."""
+    from bp_project_gb300 import _native as nat, core
+    nr, nu = shape
+    rows = np.array_split(np.arange(nr), tiles[0])
+    cols = np.array_split(np.arange(nu), tiles[1])
+    rng = np.random.default_rng(nr * nu)
+    for img in (rng.random(shape, dtype=np.float32), np.ones(shape, np.float32),
+                np.round(rng.random(shape, dtype=np.float32) * 4) / 4):
+        a = torch.from_numpy(img).cuda()
+        n = tiles[0] * tiles[1]
+        tmax = torch.empty(n, dtype=torch.float32, device="cuda")
+        first = torch.empty(n, dtype=torch.int64, device="cuda")
+        nat.check(nat.load().sarbp_tile_argmax(core._ptr(a), nr, nu, tiles[0], tiles[1], core._ptr(tmax),
+                                               core._ptr(first), core.stream_handle()), "tile_argmax")
+        want_max, want_idx = [], []
+        for r in rows:
+            for c in cols:
+                sub = img[r[0]:r[-1] + 1, c[0]:c[-1] + 1]
+                i, j = np.unravel_index(np.argmax(sub), sub.shape)
+                want_max.append(sub[i, j])
+                want_idx.append((r[0] + i) * nu + c[0] + j)
+        assert np.array_equal(tmax.cpu().numpy(), np.array(want_max, np.float32))
+        assert np.array_equal(first.cpu().numpy(), np.array(want_idx))
