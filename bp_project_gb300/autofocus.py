@@ -77,10 +77,16 @@ def sosfiltfilt(x: torch.Tensor, filt: SmoothingFilter) -> torch.Tensor:
 # ---- FP64 helpers on the device --------------------------------------------------------
 
 def _median(x: torch.Tensor, dim=None) -> torch.Tensor:
-    """numpy.median semantics (mean of the two middle values for even counts)."""
+    """numpy.median semantics: the middle value, or for even counts the mean of the two middle
+    values formed as (a + b) / 2, the way numpy averages them.  One sort along ``dim``."""
     if dim is None:
-        return torch.quantile(x.reshape(-1), 0.5)
-    return torch.quantile(x, 0.5, dim=dim)
+        x, dim = x.reshape(-1), 0
+    s = torch.sort(x, dim=dim).values
+    n = s.shape[dim]
+    upper = s.narrow(dim, n // 2, 1)
+    if n % 2:
+        return upper.squeeze(dim)
+    return ((s.narrow(dim, n // 2 - 1, 1) + upper) / 2).squeeze(dim)
 
 
 def detrend_linear(x: torch.Tensor) -> torch.Tensor:

@@ -15,9 +15,10 @@
 //
 // The recursion is serial along the pulses and the rows are independent.  One warp
 // per row: its lanes build the odd-extended row in shared memory with coalesced
-// loads, then lanes 0 and 1 (real, imaginary) run the forward pass into shared
-// memory and the backward pass out to the result, so every step of the recursion
-// reads shared memory instead of waiting on a global load.  Rows too long for
+// loads, then 2 x sections lanes (one per channel and section) run the forward pass
+// into shared memory and the backward pass out to the result, each section one
+// sample behind the one before it, so every step of the recursion reads shared
+// memory or a register instead of waiting on a global load.  Rows too long for
 // shared memory use one thread per channel with the forward pass in a time-major
 // global workspace.
 #include "common.cuh"
@@ -107,10 +108,16 @@ constexpr size_t kRowSmemLimit = 200 * 1024;
 
 size_t row_smem(int n, int padlen) { return (size_t)(n + 2 * padlen) * (sizeof(double2) + sizeof(float2)); }
 
-__global__ void __launch_bounds__(32) sosfiltfilt_row_kernel(const float* __restrict__ x, int n,
-                                                             const double* __restrict__ sos,
-                                                             const double* __restrict__ zi, int sections, int padlen,
-                                                             double* __restrict__ y) {
+// One warp per row with the cascade pipelined across lanes: lane comp * S + s (S sections, comp =
+// real / imaginary) runs section s and hands its output to lane s + 1 by a shuffle, one sample
+// behind.  A step's critical path is one section plus a shuffle instead of the whole cascade;
+// every section performs the same roundings in the same order as Biquads::step, so the result
+// is bit-identical to the one-thread-per-channel kernel.  The extended row and the forward pass
+// stay in shared memory.
+__global__ void __launch_bounds__(32) sosfiltfilt_pipe_kernel(const float* __restrict__ x, int n,
+                                                              const double* __restrict__ sos,
+                                                              const double* __restrict__ zi, int sections,
+                                                              int padlen, double* __restrict__ y) {
     extern __shared__ __align__(16) char smem[];
     const int row = blockIdx.x, lane = threadIdx.x;
     const int m = n + 2 * padlen;
@@ -119,47 +126,57 @@ __global__ void __launch_bounds__(32) sosfiltfilt_row_kernel(const float* __rest
     const float* xr = x + (size_t)row * n * 2;
     for (int i = lane; i < m; i += 32) ext[i] = make_float2(extended(xr, n, padlen, i, 0), extended(xr, n, padlen, i, 1));
     __syncwarp();
-    if (lane < 2) {
-        const int comp = lane;
-        Biquads f;
-        f.sections = sections;
-        double zs0[kMaxSections], zs1[kMaxSections];
-#pragma unroll
-        for (int s = 0; s < kMaxSections; ++s) {
-            if (s < sections) {
-                f.b0[s] = sos[6 * s];
-                f.b1[s] = sos[6 * s + 1];
-                f.b2[s] = sos[6 * s + 2];
-                f.a1[s] = sos[6 * s + 4];  // a0 == 1 (checked by the caller)
-                f.a2[s] = sos[6 * s + 5];
-                zs0[s] = zi[2 * s];
-                zs1[s] = zi[2 * s + 1];
-            }
-        }
+    const int S = sections;
+    const bool active = lane < 2 * S;
+    const int comp = active ? lane / S : 0, sec = active ? lane - comp * S : 0;
+    const unsigned mask = 2 * S >= 32 ? 0xffffffffu : (1u << (2 * S)) - 1u;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0, a1 = 0.0, a2 = 0.0, zs0 = 0.0, zs1 = 0.0, z0 = 0.0, z1 = 0.0;
+    double* fw = reinterpret_cast<double*>(fwd) + comp;
+    if (active) {
+        b0 = sos[6 * sec];
+        b1 = sos[6 * sec + 1];
+        b2 = sos[6 * sec + 2];
+        a1 = sos[6 * sec + 4];  // a0 == 1 (checked by the caller)
+        a2 = sos[6 * sec + 5];
+        zs0 = zi[2 * sec];
+        zs1 = zi[2 * sec + 1];
         const float* e = reinterpret_cast<const float*>(ext) + comp;
-        double* fw = reinterpret_cast<double*>(fwd) + comp;
         const double first = (double)e[0];
-#pragma unroll
-        for (int s = 0; s < kMaxSections; ++s) {
-            if (s < sections) {
-                f.z0[s] = __dmul_rn(zs0[s], first);
-                f.z1[s] = __dmul_rn(zs1[s], first);
+        z0 = __dmul_rn(zs0, first);
+        z1 = __dmul_rn(zs1, first);
+        double carry = 0.0;
+        for (int t = 0; t < m + S - 1; ++t) {
+            const int i = t - sec;
+            double out = 0.0;
+            if (i >= 0 && i < m) {
+                const double v = sec == 0 ? (double)e[2 * i] : carry;
+                out = __dadd_rn(__dmul_rn(b0, v), z0);
+                z0 = __dadd_rn(__dsub_rn(__dmul_rn(b1, v), __dmul_rn(a1, out)), z1);
+                z1 = __dsub_rn(__dmul_rn(b2, v), __dmul_rn(a2, out));
+                if (sec == S - 1) fw[2 * i] = out;
             }
+            carry = __shfl_up_sync(mask, out, 1);
         }
-        for (int i = 0; i < m; ++i) fw[2 * i] = f.step((double)e[2 * i]);
+    }
+    __syncwarp();
+    if (active) {
         const double last = fw[2 * (m - 1)];
-#pragma unroll
-        for (int s = 0; s < kMaxSections; ++s) {
-            if (s < sections) {
-                f.z0[s] = __dmul_rn(zs0[s], last);
-                f.z1[s] = __dmul_rn(zs1[s], last);
-            }
-        }
+        z0 = __dmul_rn(zs0, last);
+        z1 = __dmul_rn(zs1, last);
         double* yr = y + (size_t)row * n * 2 + comp;
-        for (int i = m - 1; i >= 0; --i) {
-            const double v = f.step(fw[2 * i]);
-            const int j = i - padlen;
-            if (j >= 0 && j < n) yr[2 * j] = v;
+        double carry = 0.0;
+        for (int t = 0; t < m + S - 1; ++t) {
+            const int i = m - 1 - (t - sec);
+            double out = 0.0;
+            if (t - sec >= 0 && i >= 0) {
+                const double v = sec == 0 ? fw[2 * i] : carry;
+                out = __dadd_rn(__dmul_rn(b0, v), z0);
+                z0 = __dadd_rn(__dsub_rn(__dmul_rn(b1, v), __dmul_rn(a1, out)), z1);
+                z1 = __dsub_rn(__dmul_rn(b2, v), __dmul_rn(a2, out));
+                const int j = i - padlen;
+                if (sec == S - 1 && j >= 0 && j < n) yr[2 * j] = out;
+            }
+            carry = __shfl_up_sync(mask, out, 1);
         }
     }
 }
@@ -225,6 +242,13 @@ int launch_tile_argmax(const float* a, int nr, int nu, int nr_tiles, int nu_tile
     return check_launch("tile_argmax");
 }
 
+template <class K>
+int set_smem(K kernel, size_t smem) {
+    if (smem <= 48 * 1024) return SARBP_OK;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e == cudaSuccess ? SARBP_OK : fail(SARBP_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+}
+
 size_t sosfiltfilt_workspace(int rows, int n, int padlen) {
     return (size_t)(n + 2 * padlen) * (size_t)rows * 2 * sizeof(double);
 }
@@ -233,12 +257,8 @@ int launch_sosfiltfilt(const float* x, int rows, int n, const double* sos, const
                        double* y, double* ws, cudaStream_t s) {
     const size_t smem = row_smem(n, padlen);
     if (smem <= kRowSmemLimit) {
-        if (smem > 48 * 1024) {
-            const cudaError_t e =
-                cudaFuncSetAttribute(sosfiltfilt_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-        }
-        sosfiltfilt_row_kernel<<<rows, 32, smem, s>>>(x, n, sos, zi, sections, padlen, y);
+        if (int st = set_smem(sosfiltfilt_pipe_kernel, smem)) return st;
+        sosfiltfilt_pipe_kernel<<<rows, 32, smem, s>>>(x, n, sos, zi, sections, padlen, y);
         note_launches(1);
         return check_launch("sosfiltfilt");
     }

@@ -69,3 +69,11 @@ def test_butter_lowpass_padding_matches_scipy():
     x = np.random.default_rng(1).standard_normal(64)
     # sosfiltfilt with the explicit padlen equals its default
     np.testing.assert_array_equal(signal.sosfiltfilt(f.sos, x), signal.sosfiltfilt(f.sos, x, padlen=f.padlen))
+
+
+@pytest.mark.parametrize("shape,dim", [((60,), None), ((61,), None), ((60, 2047), 0), ((59, 100), 0), ((7, 8), 1)])
+def test_median_matches_numpy_exactly(shape, dim):
+    from bp_project_gb300.autofocus import _median
+    x = np.random.default_rng(sum(shape)).standard_normal(shape)
+    est = _median(torch.from_numpy(x), dim).numpy()
+    np.testing.assert_array_equal(est, np.median(x, axis=dim))
