@@ -48,7 +48,8 @@ constexpr int kMaxChunk = 64;      // pulses per chunk of the direct kernels: tw
 constexpr int kMaxLeafChunk = 32;  // pulses per chunk of the FFBP leaf kernels: one warp computes the records
 // Window bytes per CTA: with kMaxChunk records this keeps three CTAs per SM within 227 KB.
 constexpr int kWindowBudget = 68 * 1024;
-// Lattice tiles (64 registers): four CTAs per SM.  The packed windows of a 32 x 32 tile at the
+// Lattice tiles (64 registers): four CTAs per SM (50 KB of windows, 5 KB of 80-byte records and
+// about 1 KB of static shared memory each fit the SM's 228 KB).  The packed windows of a 32 x 32 tile at the
 // usual geometries need 15-25 bins per pulse, so 64-pulse chunks still fit; wider windows
 // just fit fewer pulses per chunk.
 constexpr int kLatticeWindowBudget = 50 * 1024;
@@ -61,6 +62,7 @@ struct Rec {
     float4 b;  // u.x, u.y, 2R, frac(Q) - 1/2       (lattice: u.s_row, u.s_col, 2R, frac(Q) - 1/2)
     float4 c;  // Phi, window bias bits, window offset bits, window count - 1 bits
     float4 d;  // u.z, W_hi.z, W_lo.z                (lattice: 2 pi frac(m B_row), m u.s_row or u.x, u.y, u.z)
+    float4 e;  // lattice forward: the pairs (2R, 2R), (frac(Q) - 1/2, frac(Q) - 1/2) of packed-FP32 operands
 };
 
 struct Pix {
@@ -790,7 +792,11 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
         const float Ac = fmaf(uxf, S.sth[3], fmaf(uyf, S.sth[4], uzf * S.sth[5]));
         r.b = make_float4(Ar, Ac, 2.0f * Rf, Fm);
         // The phase step in radians; the range step (forward) or u (adjoint).
-        r.d = MODE == 1 ? make_float4(sp * kTwoPiF, m * Ar, 0.0f, 0.0f) : make_float4(sp * kTwoPiF, uxf, uyf, uzf);
+        // The forward holds its per-pulse operands as float2 pairs: (phase step, phase step),
+        // (-range step, -range step) in d and (2R, 2R), (Fm, Fm) in e.
+        const float spr = sp * kTwoPiF, nstep = -(m * Ar);
+        r.d = MODE == 1 ? make_float4(spr, spr, nstep, nstep) : make_float4(spr, uxf, uyf, uzf);
+        r.e = make_float4(2.0f * Rf, 2.0f * Rf, Fm, Fm);
     } else {
         const float sw = (float)P.scale_w, isw = (float)P.inv_scale_w;  // powers of two: exact
         r.a.x = rintf(Wx.h * isw) * sw;
@@ -802,6 +808,7 @@ __device__ __forceinline__ int make_record(const SplitParams& P, TileShared& S, 
         r.b = make_float4(uxf, uyf, 2.0f * Rf, Fm);
         r.d.x = uzf;
         r.d.w = 0.0f;
+        r.e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     r.c.x = t1;
     r.c.y = __int_as_float(kMagicBits + bo);
@@ -950,47 +957,74 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 // r0 = frac(Phi + W . delta) from the exact hi products; its other pixels are kc = -2..1
 // steps of m rows away, L = L0 + kc (m u . s_row) and phase r0 + kc frac(m W . s_row).
 // Per pixel-pulse this leaves the eps term, the window gather and the rotation.
+__device__ __forceinline__ float2 pair(float v) { return make_float2(v, v); }
+
+// The forward's per-pixel geometry runs on packed FP32 (f32x2): pixels k = 2h and 2h + 1 of
+// a thread form one float2 lane pair through the range, fraction, index and angle steps, so
+// one instruction issues both pixels' operation.  Each half rounds exactly like the scalar
+// operation, and the chain is carried with the sign of L, q2, e0 and eps flipped (negation
+// is exact, so every value equals the scalar formulation's bit for bit):
+//   -L = kc (-m u.s_row) + (-L0),  -q2 = (-L)^2 - d2,  2L + 2R = -2 (-L) + 2R,
+//   -e0 = -q2 B,  -eps = (-e0)^2 B + (-e0),  qp = ((-L) + (-eps)) (-1/dr) + Fm,
+//   s = qp - (tq - M) = (tq - M) (-1) + qp,  ang = (-kr) (-eps) + (kc sp + r0).
+// The complex cubic evaluates (re, im) as one pair; the accumulation stays scalar.
 __device__ __forceinline__ void lattice_chunk(const SplitParams& P, const Rec* __restrict__ rec,
                                               const float4* __restrict__ win, int chn, int lc, const float d2[kPX],
                                               float ar[kPX], float ai[kPX]) {
+    static_assert(kPX == 4, "two pixel pairs per thread");
     const float inv_dr = P.inv_drf, kr = P.Kf * kTwoPiF;
     const int m = kThreads >> lc, hr = (kSplitTilePixels >> lc) >> 1, cols_t = 1 << lc;
     const int tid = threadIdx.x;
     const float di = (float)((tid >> lc) + 2 * m - hr);
     const float dj = (float)((tid & (cols_t - 1)) - (cols_t >> 1));
+    const float2 nd2[2] = {make_float2(-d2[0], -d2[1]), make_float2(-d2[2], -d2[3])};
+    const float2 kcs[2] = {make_float2(-2.0f, -1.0f), make_float2(0.0f, 1.0f)};
+    const float2 ninv = pair(-inv_dr), nkr = pair(-kr), magic = pair(kMagic), nmagic = pair(-kMagic);
+    const float2 mone = pair(-1.0f), mtwo = pair(-2.0f);
 #pragma unroll 1
     for (int nl = 0; nl < chn; ++nl) {
-        const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+        const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d, re = rec[nl].e;
         const int bias = __float_as_int(rc.y);
         const unsigned last = (unsigned)__float_as_int(rc.w);
         const float4* wrow = win + 2 * __float_as_int(rc.z);
-        const float L0 = fmaf(dj, rb.y, di * rb.x);
-        const float t = fmaf(dj, ra.z, di * ra.x);  // exact
+        const float nL0 = fmaf(-dj, rb.y, -di * rb.x);  // -L0, exactly
+        const float t = fmaf(dj, ra.z, di * ra.x);       // exact
         const float r0 = ((t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x))) * kTwoPiF;  // radians
+        const float2 sp = make_float2(rd.x, rd.y), nstep = make_float2(rd.z, rd.w);
+        const float2 twoR = make_float2(re.x, re.y), fm = make_float2(re.z, re.w);
+        const float2 nL02 = pair(nL0), r02 = pair(r0);
 #pragma unroll
-        for (int k = 0; k < kPX; ++k) {
-            const float kc = (float)(k - 2);
-            const float L = fmaf(kc, rd.y, L0);
-            const float q2 = fmaf(-L, L, d2[k]);
-            const float B = rcp_approx(fmaf(2.0f, L, rb.z));
-            const float e0 = q2 * B;
-            const float eps = fmaf(-e0 * e0, B, e0);
-            const float qp = fmaf(L + eps, inv_dr, rb.w);
-            const float tq = qp + kMagic;
-            const float s = qp - (tq - kMagic);
-            const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
-            const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
-            const float vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
-            const float vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
+        for (int h = 0; h < 2; ++h) {
+            const float2 nL = __ffma2_rn(kcs[h], nstep, nL02);
+            const float2 nq2 = __ffma2_rn(nL, nL, nd2[h]);
+            const float2 den = __ffma2_rn(mtwo, nL, twoR);
+            const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+            const float2 ne0 = __fmul2_rn(nq2, B);
+            const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);
+            const float2 qp = __ffma2_rn(__fadd2_rn(nL, neps), ninv, fm);
+            const float2 tq = __fadd2_rn(qp, magic);
+            const float2 s = __ffma2_rn(__fadd2_rn(tq, nmagic), mone, qp);
             // |r0| <= 1/2 + small, |kc frac| <= 1 and K eps <= envelope / 2 turns: the angle
             // stays within +-40 rad, which the hardware sin/cos reduce themselves.
-            const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
-            float sn, cs;
-            __sincosf(ang, &sn, &cs);
-            ar[k] = fmaf(vr, cs, ar[k]);
-            ar[k] = fmaf(-vi, sn, ar[k]);
-            ai[k] = fmaf(vr, sn, ai[k]);
-            ai[k] = fmaf(vi, cs, ai[k]);
+            const float2 ang = __ffma2_rn(nkr, neps, __ffma2_rn(kcs[h], sp, r02));
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const int k = 2 * h + c;
+                const float tqc = c ? tq.y : tq.x, sc = c ? s.y : s.x;
+                const unsigned j = min((unsigned)(__float_as_int(tqc) - bias), last);
+                const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                const float2 ss = pair(sc);
+                const float2 v = __ffma2_rn(
+                    __ffma2_rn(__ffma2_rn(make_float2(c23.z, c23.w), ss, make_float2(c23.x, c23.y)), ss,
+                               make_float2(c01.z, c01.w)),
+                    ss, make_float2(c01.x, c01.y));
+                float sn, cs;
+                __sincosf(c ? ang.y : ang.x, &sn, &cs);
+                ar[k] = fmaf(v.x, cs, ar[k]);
+                ar[k] = fmaf(-v.y, sn, ar[k]);
+                ai[k] = fmaf(v.x, sn, ai[k]);
+                ai[k] = fmaf(v.y, cs, ai[k]);
+            }
         }
     }
 }
