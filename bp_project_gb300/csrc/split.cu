@@ -1296,50 +1296,66 @@ struct LatticeAdjointBody {
         const float di = (float)((tid >> lc) + 2 * m - hr);
         const float dj = (float)((tid & (cols_t - 1)) - (cols_t >> 1));
         const float mf = (float)m;
+        // The forward's packed pixel pairs (see lattice_chunk), plus R + (L + eps) as a pair.
+        const float2 nd2[2] = {make_float2(-d2[0], -d2[1]), make_float2(-d2[2], -d2[3])};
+        const float2 kcs[2] = {make_float2(-2.0f, -1.0f), make_float2(0.0f, 1.0f)};
+        const float2 ninv = pair(-inv_dr), nkr = pair(-kr), magic = pair(kMagic), nmagic = pair(-kMagic);
+        const float2 mone = pair(-1.0f), mtwo = pair(-2.0f), half = pair(0.5f);
 #pragma unroll 1
         for (int nl = 0; nl < nfit; ++nl) {
-            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
+            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d, re = rec[nl].e;
             const int bias = __float_as_int(rc.y);
             const unsigned last = (unsigned)__float_as_int(rc.w);
             const float4* wrow = win + 2 * __float_as_int(rc.z);
-            const float L0 = fmaf(dj, rb.y, di * rb.x), mA = mf * rb.x;
-            const float t = fmaf(dj, ra.z, di * ra.x);  // exact
+            const float nL0 = fmaf(-dj, rb.y, -di * rb.x), nmA = -(mf * rb.x);  // -L0, -m u.s_row: exact
+            const float t = fmaf(dj, ra.z, di * ra.x);                           // exact
             const float r0 = ((t - round_magic(t)) + fmaf(dj, ra.w, fmaf(di, ra.y, rc.x))) * kTwoPiF;
-            const float R = 0.5f * rb.z;
+            const float2 twoR = make_float2(re.x, re.y), fm = make_float2(re.z, re.w);
+            const float2 R2 = __fmul2_rn(twoR, half);
+            const float2 nL02 = pair(nL0), nstep = pair(nmA), sp = pair(rd.x), r02 = pair(r0);
             float u0 = 0.f, u1 = 0.f, t0 = 0.f, s1 = 0.f;
 #pragma unroll
-            for (int k = 0; k < kPX; ++k) {
-                const float kc = (float)(k - 2);
-                const float L = fmaf(kc, mA, L0);
-                const float q2 = fmaf(-L, L, d2[k]);
-                const float B = rcp_approx(fmaf(2.0f, L, rb.z));
-                const float e0 = q2 * B;
-                const float eps = fmaf(-e0 * e0, B, e0);
-                const float qp = fmaf(L + eps, inv_dr, rb.w);
-                const float tq = qp + kMagic;
-                const float s = qp - (tq - kMagic);
-                const unsigned j = min((unsigned)(__float_as_int(tq) - bias), last);
-                const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
-                // Horner for the value; the derivative c1 + 2 c2 s + 3 c3 s^2 = p2 + s (p1 + c3 s) reuses
-                // its partial results p1 = c3 s + c2, p2 = p1 s + c1.
-                const float pr1 = fmaf(c23.z, s, c23.x), pi1 = fmaf(c23.w, s, c23.y);
-                const float pr2 = fmaf(pr1, s, c01.z), pi2 = fmaf(pi1, s, c01.w);
-                const float vr = fmaf(pr2, s, c01.x), vi = fmaf(pi2, s, c01.y);
-                const float dvr = fmaf(s, fmaf(c23.z, s, pr1), pr2), dvi = fmaf(s, fmaf(c23.w, s, pi1), pi2);
-                const float ang = fmaf(kr, eps, fmaf(kc, rd.x, r0));
-                float sn, cs;
-                __sincosf(ang, &sn, &cs);
-                // h = conj(G) exp(i phi): U += v h, and the position weight
-                // Re(conj(G) (v'/dr + i k v) exp(i phi)) / d = (Re(v' h) / dr - k Im(v h)) / d.
-                const float gr = gre[k], gi = gim[k];
-                const float hr = fmaf(gr, cs, gi * sn), hi = fmaf(gr, sn, -gi * cs);
-                u0 = fmaf(vr, hr, fmaf(-vi, hi, u0));
-                const float w1 = fmaf(vr, hi, vi * hr);
-                u1 += w1;
-                const float q = fmaf(dvr, hr, -dvi * hi);
-                const float tt = fmaf(q, inv_dr, -kr * w1) * rcp_approx(R + (L + eps));
-                t0 += tt;
-                s1 = fmaf(kc, tt, s1);
+            for (int h = 0; h < 2; ++h) {
+                const float2 nL = __ffma2_rn(kcs[h], nstep, nL02);
+                const float2 nq2 = __ffma2_rn(nL, nL, nd2[h]);
+                const float2 den = __ffma2_rn(mtwo, nL, twoR);
+                const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+                const float2 ne0 = __fmul2_rn(nq2, B);
+                const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);
+                const float2 nLe = __fadd2_rn(nL, neps);  // -(L + eps)
+                const float2 qp = __ffma2_rn(nLe, ninv, fm);
+                const float2 tq = __fadd2_rn(qp, magic);
+                const float2 s = __ffma2_rn(__fadd2_rn(tq, nmagic), mone, qp);
+                const float2 ang = __ffma2_rn(nkr, neps, __ffma2_rn(kcs[h], sp, r02));
+                const float2 dist = __ffma2_rn(nLe, mone, R2);  // R + (L + eps)
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const int k = 2 * h + c;
+                    const float kc = (float)(k - 2);
+                    const float tqc = c ? tq.y : tq.x;
+                    const unsigned j = min((unsigned)(__float_as_int(tqc) - bias), last);
+                    const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                    // Horner for the value as (re, im) pairs; the derivative c1 + 2 c2 s + 3 c3 s^2 =
+                    // p2 + s (p1 + c3 s) reuses its partial results p1 = c3 s + c2, p2 = p1 s + c1.
+                    const float2 ss = pair(c ? s.y : s.x), c3 = make_float2(c23.z, c23.w);
+                    const float2 p1 = __ffma2_rn(c3, ss, make_float2(c23.x, c23.y));
+                    const float2 p2 = __ffma2_rn(p1, ss, make_float2(c01.z, c01.w));
+                    const float2 v = __ffma2_rn(p2, ss, make_float2(c01.x, c01.y));
+                    const float2 dv = __ffma2_rn(ss, __ffma2_rn(c3, ss, p1), p2);
+                    float sn, cs;
+                    __sincosf(c ? ang.y : ang.x, &sn, &cs);
+                    // h = conj(G) exp(i phi): U += v h, and the position weight
+                    // Re(conj(G) (v'/dr + i k v) exp(i phi)) / d = (Re(v' h) / dr - k Im(v h)) / d.
+                    const float gr = gre[k], gi = gim[k];
+                    const float hr = fmaf(gr, cs, gi * sn), hi = fmaf(gr, sn, -gi * cs);
+                    u0 = fmaf(v.x, hr, fmaf(-v.y, hi, u0));
+                    const float w1 = fmaf(v.x, hi, v.y * hr);
+                    u1 += w1;
+                    const float q = fmaf(dv.x, hr, -dv.y * hi);
+                    const float tt = fmaf(q, inv_dr, -kr * w1) * rcp_approx(c ? dist.y : dist.x);
+                    t0 += tt;
+                    s1 = fmaf(kc, tt, s1);
+                }
             }
             float sq, s4;
             warp_sum5(u0, u1, t0, fmaf(di, t0, mf * s1), dj * t0, sq, s4);
