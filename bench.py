@@ -43,7 +43,7 @@ REF_SAMPLE_PIXELS = 131072          # pixels per step of the reference arm (~1 s
 # DRAM bytes (read + write) of one split_lattice_kernel launch on this workload, from an ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum): only the ~920 range bins per pulse that the scene spans
 # are read, so traffic is far below the algorithmic 302 MB.
-NCU_TRAFFIC_BYTES = 33.299456e6 + 83.196160e6  # 4 pulse splits: the partial images are written
+NCU_TRAFFIC_BYTES = 32.980992e6 + 83.194880e6  # 4 pulse splits: the partial images are written
 L2_FLUSH_BYTES = 256 << 20          # written between timed steps: twice GB300's 129 MB L2
 
 
