@@ -33,7 +33,8 @@ def _all_kernels(scene, data, pos, wt, ph, dev):
     """One call of every product kernel on the scene (small scenes keep this to tens of ms)."""
     import numpy as np
 
-    from .autofocus import butter_lowpass, image_entropy, sosfiltfilt
+    from .autofocus import butter_lowpass, image_entropy, pick_targets, sosfiltfilt
+    from .ffbp import PolarImage
     from .autograd import backproject_lattice
     from .sar_io import range_compress
     cfg, lat = scene.config, scene.lattice
@@ -65,6 +66,7 @@ def _all_kernels(scene, data, pos, wt, ph, dev):
         for m, prog in progs.items():
             polar = prog.execute(data, pos, wt, ph, scene.range_start, scene.data_dr, scene.k)
         core.evaluate_lattice(polar, grid, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols, scene.k)
+        pick_targets(PolarImage(polar, plan.origin.copy(), plan.r0, plan.dr, plan.u0, plan.du, 1))
         core.evaluate_image(polar, grid, pts, scene.k)
         contrib = core.target_contributions(data, pos, targets, scene.range_start, scene.data_dr, scene.k)
         sosfiltfilt(contrib, butter_lowpass(12.0, cfg.prf))
