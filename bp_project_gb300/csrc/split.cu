@@ -48,11 +48,12 @@ constexpr int kMaxChunk = 64;      // pulses per chunk of the direct kernels: tw
 constexpr int kMaxLeafChunk = 32;  // pulses per chunk of the FFBP leaf kernels: one warp computes the records
 // Window bytes per CTA: with kMaxChunk records this keeps three CTAs per SM within 227 KB.
 constexpr int kWindowBudget = 68 * 1024;
-// Lattice tiles (64 registers): four CTAs per SM (50 KB of windows, 5 KB of 80-byte records and
-// about 1 KB of static shared memory each fit the SM's 228 KB).  The packed windows of a 32 x 32 tile at the
-// usual geometries need 15-25 bins per pulse, so 64-pulse chunks still fit; wider windows
-// just fit fewer pulses per chunk.
-constexpr int kLatticeWindowBudget = 50 * 1024;
+// Lattice tiles (64 registers): four CTAs per SM.  Per CTA, 49 KB of windows, 5 KB of 80-byte
+// records, up to 1.25 KB of static shared memory (the batch kernel) and the 1 KB the runtime
+// reserves: 4 x 56.25 KB fits the SM's 228 KB.  The packed windows of a 32 x 32 tile at the
+// usual geometries need 15-25 bins per pulse, so 64-pulse chunks mostly fit; wider windows
+// just fit fewer pulses per chunk (the image does not depend on the chunking).
+constexpr int kLatticeWindowBudget = 49 * 1024;
 // K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
 // error, FFBP leaves 1e-4.
 constexpr double kDirectEnvelope = 8.0;

@@ -79,6 +79,10 @@ def test_batch_equals_single_scene_paths(small_batch):
         kinds.append(type(sc).__name__)
     assert "DirectScene" in kinds and "FFBPScene" in kinds
     print(batch.info, "launches", batch.launch_count)
+    # The persistent direct launch keeps the single-scene lattice kernel's four CTAs per SM.
+    n_direct = sum(-(-sc.rows // 32) * -(-sc.cols // 32) for sc in small_batch if type(sc).__name__ == "DirectScene")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert batch.info["bp_blocks"] == min(n_direct, 4 * sms), (batch.info, n_direct, sms)
     assert batch.launch_count == 1 + 4 + 1 + batch.info["max_height"]  # memset, prologues + leaves, direct, merges
     # graph capture + replay reproduce the eager result
     first = [o.clone() for o in batch.outputs]
