@@ -623,6 +623,33 @@ def main():
         torch.cuda.synchronize()
         ffbp_ms = f0.elapsed_time(f1) / nrep
         g = ground.cpu().numpy().reshape(lat.rows, lat.cols).astype(np.complex128)
+        # Direct BP onto the FFBP root's polar grid: the surface of the reference's CudaBaseline.run_direct
+        # (split precision, one pulse pass per tile), and the FFBP image against it on that grid.
+        polar_direct = torch.empty((grid.nr, grid.nu), dtype=torch.complex64, device=dev)
+
+        def polar_step():
+            return core.direct_polar(data, pos, wt, ph, grid, scene.range_start, scene.data_dr, scene.k, mode="split",
+                                     out=polar_direct)
+
+        polar_step()
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for _ in range(2):
+            polar_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        polar_ms = f0.elapsed_time(f1) / 2
+        polar_ffbp = ffbp_step()
+        torch.cuda.synchronize()
+        diff = (polar_ffbp.to(torch.complex128) - polar_direct.to(torch.complex128)).abs().pow(2).sum()
+        norm = polar_direct.to(torch.complex128).abs().pow(2).sum()
+        extra["polar_direct"] = {
+            "gpix_pulse_s": grid.nr * grid.nu * cfg.pulses / (polar_ms / 1e3) / 1e9, "ms": polar_ms,
+            "grid": [grid.nr, grid.nu], "pulses": cfg.pulses,
+            "ffbp_vs_direct_err_polar": float(torch.sqrt(diff / norm)),
+            "what": "core.direct_polar (sarbp_direct_polar, the CudaBaseline.run_direct path) onto the FFBP root's "
+                    "cropped polar grid, split precision, one pulse pass per tile"}
+        del polar_direct, polar_ffbp
         extra.update({
             "ffbp_img_per_s": 1e3 / ffbp_ms, "ffbp_ms": ffbp_ms,
             "ffbp_config": f"leaf {cfg.leaf_size}, {plan.counts['leaves']} leaves, {plan.counts['merges']} merges, "
