@@ -1,9 +1,10 @@
 """Many scenes in one schedule: persistent work-queue kernels over uneven scenes.
 
 ``SceneBatch`` binds a list of scenes (direct BP onto a flat lattice, or FFBP
-of a planned tree) to ``sarbp_batch_*``: all direct tiles and FFBP leaf tiles
-run in one persistent launch that drains a largest-first work queue, and the
-FFBP merges run as one persistent launch per tree height across all scenes.
+of a planned tree) to ``sarbp_batch_*``: all scenes' direct tiles run in one
+persistent launch that drains a largest-first work queue, all FFBP leaf tiles in
+a second one, and the FFBP merges as one persistent launch per tree height
+across all scenes.
 ``execute`` only enqueues work on the current stream (no allocation, no
 synchronisation), so the whole batch can be captured in one CUDA graph
 (``capture_graph`` / ``replay``), like ``ResidentProgram``.
@@ -123,6 +124,8 @@ class SceneBatch:
     def scene_latencies_ms(self):
         """Per-scene completion times (ms from the batch's start) of one traced execution: each
         work item raises its scene's slot to the GPU's nanosecond timer when it finishes."""
+        if self._handle is None:
+            raise RuntimeError("batch is closed")
         lib = nat.load()
         trace = torch.zeros(len(self.scenes) + 1, dtype=torch.int64, device=self.workspace.device)
         nat.check(lib.sarbp_batch_set_trace(self._handle, core._ptr(trace)), "batch_set_trace")
