@@ -141,6 +141,17 @@ def cpu_baseline(scene, pixels, seed=11):
                       f"(FP64 C++/OpenMP restatement of ffbp.backproject_points)"}, idx, out
 
 
+def replica_rate(total_ms, units, steps, world, dist=None, device=None):
+    """Whole-job rate of ``world`` independent replicas: the slowest rank's timed total (max over
+    ranks, so every rank returns the same) and all ranks' units.  Returns (total_ms, Gunits/s)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * units * steps / (total_ms / 1e3) / 1e9
+
+
 def run_reference(args, rank):
     """Reference arm: the reference's CPU BP (restated, FP64, all host threads) on a bounded sample per step."""
     if rank != 0:
@@ -507,13 +518,8 @@ def main():
         barrier()
     launches = _native.launch_count() - launches0
     per_launch_ms = [ev0[i].elapsed_time(ev1[i]) for i in range(args.steps)]
-    total_ms = sum(per_launch_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = replica_rate(sum(per_launch_ms), units, args.steps, world, dist, dev)
     ms_per_step = total_ms / args.steps
-    value = world * units * args.steps / (total_ms / 1e3) / 1e9
     image = out.cpu().numpy()
 
     # End to end through the public API: every step copies its inputs from pinned host memory to the
@@ -564,7 +570,8 @@ def main():
     stream.wait_stream(down_stream)  # the last image is back on the host
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_total, e2e_value = replica_rate(e0.elapsed_time(e1), units, args.steps, world, dist, dev)
+    e2e_ms = e2e_total / args.steps
     host_out = host_outs[0]
     h2d = sum(t.numel() * t.element_size() for t in (host_data, host_pos, host_w, host_ph))
     d2h = host_out.numel() * host_out.element_size()
@@ -688,7 +695,7 @@ def main():
                    "pulse_split": core.lattice_pulse_split(lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
                                                            "split"),
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": world * units / (e2e_ms / 1e3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                 "path": "every step: pinned host data/pos/weight/phase -> device, core.backproject_lattice (C ABI), "
                         "image -> pinned host; uploads and read-backs on their own streams overlap the "
