@@ -32,11 +32,14 @@ def test_replica_rate_takes_the_slowest_rank():
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
     world, times = 2, [800.0, 1000.0]  # ms for 4 steps on each rank
-    out = mp.Manager().dict()
+    manager = mp.get_context("spawn").Manager()  # no fork of a multi-threaded process
+    out = manager.dict()
     mp.start_processes(_rank, args=(world, port, times, out), nprocs=world, join=True, start_method="spawn")
-    assert len(out) == world
+    results = dict(out)
+    manager.shutdown()
+    assert len(results) == world
     for rank in range(world):
-        total, rate = out[rank]
+        total, rate = results[rank]
         assert total == 1000.0
         assert rate == pytest.approx(world * 1e9 * 4 / 1.0 / 1e9)
 
