@@ -77,3 +77,19 @@ def test_median_matches_numpy_exactly(shape, dim):
     x = np.random.default_rng(sum(shape)).standard_normal(shape)
     est = _median(torch.from_numpy(x), dim).numpy()
     np.testing.assert_array_equal(est, np.median(x, axis=dim))
+
+
+def test_rounded_sosfiltfilt_restatement_equals_scipy():
+    """The separately rounded forward-backward recursion that the GPU filter test compares against
+    bit for bit equals scipy.signal.sosfiltfilt on this host."""
+    from scipy import signal
+
+    from bp_project_gb300.autofocus import butter_lowpass
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from test_gpu_autofocus import _sosfiltfilt_rounded
+    rng = np.random.default_rng(3)
+    x = (rng.standard_normal((5, 400)) + 1j * rng.standard_normal((5, 400))).astype(np.complex64)
+    for cutoff in (12.0, 1.0):
+        f = butter_lowpass(cutoff, 1000.0)
+        np.testing.assert_array_equal(_sosfiltfilt_rounded(f.sos, f.zi, f.padlen, x),
+                                      signal.sosfiltfilt(f.sos, x, axis=1))
