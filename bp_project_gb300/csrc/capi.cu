@@ -43,6 +43,9 @@ size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 bool is_finite_value(double v) { return isfinite(v) != 0; }
 
+}  // namespace
+
+// Argument checks and descriptor builders shared by every entry point (declared in common.cuh).
 int check_pulses(const float* data, int pulses, int samples, const double* pos, const double* weight,
                  const double* phase, double data_dr, double k) {
     if (!data || !pos || !weight || !phase) return fail(SARBP_ERR_TYPE, "data, pos, weight and phase must be device pointers");
@@ -109,6 +112,23 @@ PulseInputs inputs_of(const float* data, int pulses, int samples, const double* 
     return in;
 }
 
+int split_direct_polar(const PulseInputs& in, const sarbp_polar_grid& grid, int chunk_pulses, int pulse_split,
+                       float2* parts, float2* out, cudaStream_t s) {
+    PolarDesc g = desc_of(grid);
+    g.a = 0;
+    g.b = in.pulses;
+    const long long npix = (long long)grid.nr * grid.nu;
+    double radius = 0.0;
+    g.tile_lc = split_polar_tile_lc(g, &radius);
+    const int wb = split_window_bins(radius, in.data_dr);
+    const int ch = split_chunk_for(wb, chunk_pulses);
+    int st = launch_split_polar(in, g, pulse_split, ch, wb, pulse_split > 1 ? parts : out, g.nu, npix, s);
+    if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(parts, pulse_split, npix, npix, out, s);
+    return st;
+}
+
+
+namespace {
 
 // Window radius assumed for point tiles: pulses of wider tiles run through the two-float fallback.
 constexpr double kPointRadius = 24.0;
@@ -175,26 +195,18 @@ int sarbp_direct_polar(const float* data, int pulses, int samples, const double*
         return fail(SARBP_ERR_WORKSPACE, "direct_polar needs %zu workspace bytes", need);
     cudaStream_t s = (cudaStream_t)stream;
     const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    float2* dst = reinterpret_cast<float2*>(out);
+    float2* parts = pulse_split > 1 ? reinterpret_cast<float2*>(workspace) : dst;
+    if (mode == SARBP_SPLIT) return split_direct_polar(in, *grid, chunk_pulses, pulse_split, parts, dst, s);
     PolarDesc g = desc_of(*grid);
     g.a = 0;
     g.b = pulses;
-    float2* dst = reinterpret_cast<float2*>(out);
-    float2* parts = pulse_split > 1 ? reinterpret_cast<float2*>(workspace) : dst;
     const long long npix = (long long)grid->nr * grid->nu;
-    int st;
-    if (mode == SARBP_SPLIT) {
-        double radius = 0.0;
-        g.tile_lc = split_polar_tile_lc(g, &radius);
-        const int wb = split_window_bins(radius, data_dr);
-        const int ch = split_chunk_for(wb, chunk_pulses);
-        st = launch_split_polar(in, g, pulse_split, ch, wb, parts, g.nu, npix, s);
-    } else {
-        st = SARBP_OK;
-        for (int part = 0; part < pulse_split && st == SARBP_OK; ++part) {
-            const int p0 = (int)((long long)pulses * part / pulse_split);
-            const int p1 = (int)((long long)pulses * (part + 1) / pulse_split);
-            st = launch_plain_polar(mode, in, g, p0, p1, chunk_pulses, parts + part * npix, g.nu, s);
-        }
+    int st = SARBP_OK;
+    for (int part = 0; part < pulse_split && st == SARBP_OK; ++part) {
+        const int p0 = (int)((long long)pulses * part / pulse_split);
+        const int p1 = (int)((long long)pulses * (part + 1) / pulse_split);
+        st = launch_plain_polar(mode, in, g, p0, p1, chunk_pulses, parts + part * npix, g.nu, s);
     }
     if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(parts, pulse_split, npix, npix, dst, s);
     return st;

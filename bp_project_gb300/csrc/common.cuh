@@ -127,6 +127,21 @@ struct PulseInputs {
     double range_start, data_dr, k;
 };
 
+// ---- argument checks and descriptors shared by the entry points (capi.cu) ------
+// Each returns SARBP_OK or a status with the message recorded for sarbp_last_error.
+int check_pulses(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                 const double* phase, double data_dr, double k);
+int check_mode(int mode);
+int check_grid(const sarbp_polar_grid* g);
+PolarDesc desc_of(const sarbp_polar_grid& g);
+PulseInputs inputs_of(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                      const double* phase, double range_start, double data_dr, double k);
+// Split-precision direct BP onto a polar grid over all pulses: the tile shape, window and chunk
+// choice of sarbp_direct_polar(mode = SARBP_SPLIT).  With pulse_split > 1 the partial images go to
+// `parts` ([pulse_split, nr, nu]) and are summed in fixed order into `out`.
+int split_direct_polar(const PulseInputs& in, const sarbp_polar_grid& grid, int chunk_pulses, int pulse_split,
+                       float2* parts, float2* out, cudaStream_t s);
+
 // Plain (reference-arithmetic) kernels.
 int launch_plain_polar(int mode, const PulseInputs& in, const PolarDesc& g, int pulse_begin, int pulse_end,
                        int chunk, float2* out, long long out_stride, cudaStream_t s);

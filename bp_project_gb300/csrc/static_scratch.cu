@@ -25,7 +25,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 float2* g_scratch_address[kMaxDevices] = {};
 
-// Device address of g_static_scratch on the current device, looked up once per device.
+// Device address of g_static_scratch on the current device, looked up once per device.  The
+// cached address does not survive cudaDeviceReset (the module, and with it the array, is loaded
+// again afterwards); a process that resets a device must not call the static entry point on it
+// again.
 int static_scratch(float2** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -55,63 +58,29 @@ size_t sarbp_static_scratch_elements(void) { return kStaticScratchElems; }
 int sarbp_direct_polar_static(const float* data, int pulses, int samples, const double* pos, const double* weight,
                               const double* phase, const sarbp_polar_grid* grid, double range_start, double data_dr,
                               double k, int chunk_pulses, int pulse_split, float* out, void* stream) {
-    if (!data || !pos || !weight || !phase || !grid || !out)
-        return fail(SARBP_ERR_TYPE, "data, pos, weight, phase, grid and out must not be NULL");
-    if (pulses < 1 || samples < 1) return fail(SARBP_ERR_VALUE, "pulses and samples must be positive");
-    if (grid->nr <= 0 || grid->nu <= 0) return fail(SARBP_ERR_VALUE, "empty image grids are unsupported");
-    if (grid->side != 1 && grid->side != -1) return fail(SARBP_ERR_VALUE, "side must be +1 or -1");
-    if (!isfinite(data_dr) || data_dr == 0.0 || !isfinite(k)) return fail(SARBP_ERR_VALUE, "data_dr and k must be finite, data_dr non-zero");
+    // The same checks, in the same order, as sarbp_direct_polar(mode = SARBP_SPLIT).
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (int st = check_grid(grid)) return st;
+    if (!out) return fail(SARBP_ERR_TYPE, "out must not be NULL");
     if (chunk_pulses <= 0) return fail(SARBP_ERR_VALUE, "chunk_pulses must be positive");
     if (pulse_split < 1 || pulse_split > pulses) return fail(SARBP_ERR_VALUE, "pulse_split must be in [1, pulses]");
+    // nr * nu fits 63 bits (both are positive ints); compare against the capacity divided by the
+    // split so that no product can wrap.
     const long long npix = (long long)grid->nr * grid->nu;
-    if (pulse_split > 1 && (unsigned long long)npix * (unsigned long long)pulse_split > kStaticScratchElems)
+    if (pulse_split > 1 && npix > (long long)(kStaticScratchElems / (size_t)pulse_split))
         return fail(SARBP_ERR_VALUE,
-                    "pulse_split * nr * nu = %lld exceeds the static scratch of %zu complex64 values; "
+                    "pulse_split * nr * nu = %d * %lld exceeds the static scratch of %zu complex64 values; "
                     "use sarbp_direct_polar with a workspace",
-                    npix * pulse_split, kStaticScratchElems);
+                    pulse_split, npix, kStaticScratchElems);
     float2* scratch = nullptr;
     if (pulse_split > 1) {
         if (int st = static_scratch(&scratch)) return st;
     }
-    PulseInputs in;
-    in.data = reinterpret_cast<const float2*>(data);
-    in.pulses = pulses;
-    in.samples = samples;
-    in.pos = pos;
-    in.weight = weight;
-    in.phase = phase;
-    in.range_start = range_start;
-    in.data_dr = data_dr;
-    in.k = k;
-    PolarDesc g{};
-    g.ox = grid->origin[0];
-    g.oy = grid->origin[1];
-    g.oz = grid->origin[2];
-    g.r0 = grid->r0;
-    g.dr = grid->dr;
-    g.u0 = grid->u0;
-    g.du = grid->du;
-    g.nr = grid->nr;
-    g.nu = grid->nu;
-    g.side = grid->side;
-    g.a = 0;
-    g.b = pulses;
-    g.left = g.right = -1;
-    g.win_nr = grid->nr;
-    g.win_nu = grid->nu;
-    g.out_stride = grid->nu;
-    split_geometry(g);
-    double radius = 0.0;
-    g.tile_lc = split_polar_tile_lc(g, &radius);
-    const int wb = split_window_bins(radius, data_dr);
-    const int ch = split_chunk_for(wb, chunk_pulses);
-    cudaStream_t s = (cudaStream_t)stream;
-    float2* dst = reinterpret_cast<float2*>(out);
-    // Every partial image is fully overwritten by the split kernel, so the
-    // scratch needs no clearing between calls.
-    int st = launch_split_polar(in, g, pulse_split, ch, wb, pulse_split > 1 ? scratch : dst, g.nu, npix, s);
-    if (st == SARBP_OK && pulse_split > 1) st = launch_sum_parts(scratch, pulse_split, npix, npix, dst, s);
-    return st;
+    // Every partial image is fully overwritten by the split kernel, so the scratch needs no
+    // clearing between calls.
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    return split_direct_polar(in, *grid, chunk_pulses, pulse_split, scratch, reinterpret_cast<float2*>(out),
+                              (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -136,11 +136,15 @@ int sarbp_direct_polar(const float* data, int pulses, int samples, const double*
  * cudaMalloc would synchronise, cgo/JNI hosts that only see the buffers they
  * were handed).  Limit: pulse_split * nr * nu <= sarbp_static_scratch_elements()
  * (2^21 complex64, 16 MiB, held by every GPU that loads the library until
- * exit); larger requests fail with SARBP_ERR_VALUE.  The first call on a device
- * looks up the array's device address and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * Nothing in the array needs clearing: each call overwrites what it reads. */
+ * exit); larger requests fail with SARBP_ERR_VALUE.  Arguments are checked
+ * exactly as sarbp_direct_polar checks them (alignment, finite geometry) before
+ * anything reaches the GPU.  The first call on a device looks up the array's
+ * device address and should come before any stream capture; the address is
+ * kept for the life of the process, so a device that the process resets with
+ * cudaDeviceReset must not be used with this entry point again.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Nothing in the array
+ * needs clearing: each call overwrites what it reads. */
 size_t sarbp_static_scratch_elements(void);
 int sarbp_direct_polar_static(const float* data, int pulses, int samples, const double* pos,
                               const double* weight, const double* phase, const sarbp_polar_grid* grid,

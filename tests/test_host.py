@@ -228,3 +228,37 @@ def test_lattice_detection_for_point_lists():
     nudged[500, 0] += 1e-6
     assert lattice_of(nudged) is None
     assert lattice_of(pts[:1000]) is None  # not whole rows
+
+
+def test_static_entry_point_checks_like_the_workspace_entry_point(lib):
+    """The allocation-free entry point rejects misaligned pointers, non-finite grids and
+    oversized splits with the workspace entry point's statuses, before any GPU call."""
+    h = lib.load()
+    fake = ctypes.c_void_p(0x10000)  # never dereferenced: validation fails first
+    odd = ctypes.c_void_p(0x10004)   # 4-byte aligned only
+    g = lib.polar_grid((0, 0, 10), 100.0, 0.5, 16, -0.1, 0.01, 16, 1)
+
+    def both(data, grid, split=1, chunk=64):
+        a = h.sarbp_direct_polar(data, 8, 64, fake, fake, fake, ctypes.byref(grid), 90.0, 0.5, -50.0, 3, chunk,
+                                 split, fake, fake, 1 << 30, None)
+        b = h.sarbp_direct_polar_static(data, 8, 64, fake, fake, fake, ctypes.byref(grid), 90.0, 0.5, -50.0, chunk,
+                                        split, fake, None)
+        return a, b
+
+    assert both(odd, g) == (lib.SARBP_ERR_TYPE, lib.SARBP_ERR_TYPE)
+    assert b"aligned" in h.sarbp_last_error()
+    for field in ("r0", "dr", "u0", "du"):
+        bad = lib.polar_grid((0, 0, 10), 100.0, 0.5, 16, -0.1, 0.01, 16, 1)
+        setattr(bad, field, float("nan"))
+        assert both(fake, bad) == (lib.SARBP_ERR_VALUE, lib.SARBP_ERR_VALUE), field
+        assert b"finite" in h.sarbp_last_error()
+    bad = lib.polar_grid((float("inf"), 0, 10), 100.0, 0.5, 16, -0.1, 0.01, 16, 1)
+    assert both(fake, bad) == (lib.SARBP_ERR_VALUE, lib.SARBP_ERR_VALUE)
+    assert both(fake, g, chunk=0) == (lib.SARBP_ERR_VALUE, lib.SARBP_ERR_VALUE)
+    assert both(fake, g, split=9) == (lib.SARBP_ERR_VALUE, lib.SARBP_ERR_VALUE)
+    # A split whose product with nr * nu would wrap 64 bits is refused, not wrapped past the check.
+    huge = lib.polar_grid((0, 0, 10), 100.0, 0.5, 1 << 30, -0.1, 0.01, 1 << 30, 1)
+    st = h.sarbp_direct_polar_static(fake, 1 << 20, 64, fake, fake, fake, ctypes.byref(huge), 90.0, 0.5, -50.0, 64,
+                                     1 << 4, fake, None)
+    assert st == lib.SARBP_ERR_VALUE
+    assert b"exceeds the static scratch" in h.sarbp_last_error()
