@@ -7,7 +7,17 @@ synthetic scene (25 point targets over clutter scatterers).  Also reported:
 FFBP on the same scene (leaves of 16 pulses, 8 merge levels) in images/s,
 errors against the FP64 oracle, the plain FP64-phase kernel on the same
 pixels, the CPU oracle on a bounded pixel sample, and the roofline of the
-dominant kernel.
+dominant kernel.  The same line carries, each with the clocks sampled while it
+ran:
+
+* ``c2_direct``: split direct BP on the 30 km precision-stress scene (8192
+  pulses x 16384 bins -> 4096^2 lattice at 0.25 m) and its sampled error vs FP64;
+* ``autofocus``: on the 2048-pulse / 1024^2 scene with navigation errors, the
+  reference's phase-gradient autofocus on the CPU oracle (its seconds and the
+  entropy it reaches), the GPU port of that loop, and the gradient entropy
+  autofocus's wall time to the same entropy, for a rough and a smooth error model;
+* ``batch``: 64 uneven scenes as one CUDA graph against the same scenes formed
+  one at a time (ms per graph, speed-up, per-scene latency spread).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
     python bench.py --workload autofocus     # autofocus wall time on the 2048-pulse scene
@@ -57,6 +67,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ffbp", action="store_true")
     ap.add_argument("--no-autofocus", action="store_true")
+    ap.add_argument("--no-c2", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--workload", choices=("direct", "autofocus", "batch"), default="direct")
     ap.add_argument("--scenes", type=int, default=64)
     return ap.parse_args()
@@ -231,19 +243,18 @@ def autofocus_case(dev, walk_sigma):
 
     phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent, cfg.prf, cutoffs=(12,),
                              **pga_args)  # warm-up
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    gpu_pos, gpu_records = phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent,
-                                                    cfg.prf, **pga_args)
-    torch.cuda.synchronize()
-    gpu_pga_s = time.perf_counter() - t0
-    e_gpu_pga = entropy(gpu_pos)
-
     entropy_autofocus(d, nav_t, w, ph, *geo, steps=2)  # warm-up
     torch.cuda.synchronize()
-    to_target = entropy_autofocus(d, nav_t, w, ph, *geo, steps=500, target_entropy=e_ref, time_limit=120)
-    t_target = to_target.history[-1][0]
-    full = entropy_autofocus(d, nav_t, w, ph, *geo, steps=100)
+    with Clocks(dev.index or 0) as clocks:
+        t0 = time.perf_counter()
+        gpu_pos, gpu_records = phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent,
+                                                        cfg.prf, **pga_args)
+        torch.cuda.synchronize()
+        gpu_pga_s = time.perf_counter() - t0
+        to_target = entropy_autofocus(d, nav_t, w, ph, *geo, steps=500, target_entropy=e_ref, time_limit=120)
+        t_target = to_target.history[-1][0]
+        full = entropy_autofocus(d, nav_t, w, ph, *geo, steps=100)
+    e_gpu_pga = entropy(gpu_pos)
     return {
         "errors": f"2 cm LOS sinusoid (3 periods), {walk_sigma * 1e3:g} mm/pulse random walk (detrended), "
                   f"3*pi quadratic phase in the data",
@@ -258,38 +269,80 @@ def autofocus_case(dev, walk_sigma):
         "entropies": {"initial": entropy(nav), "true_track": entropy(sc.position), "reference_pga": e_ref,
                       "gpu_pga": e_gpu_pga, "entropy_autofocus": full.entropy},
         "speedup_vs_reference_pga": ref_s / t_target,
+        "speedup_vs_gpu_pga": gpu_pga_s / t_target,
+        "clocks": clocks.summary(),
     }
 
 
-def autofocus_rates(dev):
-    """Autofocus iterations per second on the 2048-pulse scene (GPU only; the CPU comparison is
-    ``--workload autofocus``): the reference's phase-gradient loop (FFBP + target picking + update per
-    iteration) and the gradient entropy autofocus (one forward + adjoint BP per evaluation)."""
+def autofocus_wall(dev):
+    """Wall time of the gradient entropy autofocus to the entropy that the reference's phase-gradient
+    autofocus reaches (CPU oracle, all host threads), beside the GPU port of that loop, for the full
+    error model (with the 1 mm/pulse random walk) and a smooth one (without it)."""
+    rough = autofocus_case(dev, 1e-3)
+    smooth = autofocus_case(dev, 0.0)
+    return {
+        "pga_iters_per_s": rough["gpu_pga"]["iters_per_s"],
+        "entropy_evals_per_s": rough["entropy_autofocus"]["final_evaluations"]
+        / rough["entropy_autofocus"]["final_seconds"],
+        "seconds_to_reference_entropy": {"rough": rough["entropy_autofocus"]["seconds_to_reference_entropy"],
+                                         "smooth": smooth["entropy_autofocus"]["seconds_to_reference_entropy"]},
+        "workload": "2048 pulses x 4096 bins, 1024^2 lattice @0.5 m, 16 targets + 1024 clutter; PGA: FFBP (leaf "
+                    "64) + 12x12 target picks + estimate_update per iteration; entropy: forward + adjoint BP per "
+                    "L-BFGS evaluation",
+        "rough": rough, "smooth": smooth,
+    }
+
+
+def c2_direct(dev, steps, warmup, sample_pixels=16384, seed=13):
+    """Split direct BP on the 30 km precision-stress scene (8192 pulses x 16384 bins -> 4096^2 lattice at
+    0.25 m): throughput with a flushed L2 before every step, and the error against the FP64 oracle on a
+    random pixel sample."""
     import torch
 
-    from bp_project_gb300.autofocus import entropy_autofocus, phase_gradient_autofocus
-    sc, data, nav, weight, phase = autofocus_scene(str(dev))
-    cfg, lat = sc.config, sc.lattice
-    d, w, ph = (torch.from_numpy(a).to(dev) for a in (data, weight, phase))
-    nav_t = torch.from_numpy(nav).to(dev)
-    pga = dict(side=1, leaf_size=64, range_spacing=0.5, angular_oversample=2.0, weight=weight)
-    phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent, cfg.prf, cutoffs=(12,), **pga)
-    torch.cuda.synchronize()
+    from bp_project_gb300 import core, scenes
+    from oracle import reference as ora
+    cfg = scenes.CONFIGS["c2"]
     t0 = time.perf_counter()
-    _, records = phase_gradient_autofocus(d, nav_t, sc.range_start, sc.data_dr, cfg.fc, sc.extent, cfg.prf, **pga)
+    sc = scenes.synthesize(cfg, device=str(dev))
+    synth_s = time.perf_counter() - t0
+    lat = sc.lattice
+    data = torch.from_numpy(sc.data).to(dev)
+    pos, wt, ph = (torch.from_numpy(a).to(dev) for a in (sc.position, sc.weight, sc.phase))
+    out = torch.empty((lat.rows, lat.cols), dtype=torch.complex64, device=dev)
+
+    def step():
+        core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                 sc.range_start, sc.data_dr, sc.k, mode="split", out=out)
+
+    for _ in range(max(warmup, 3)):
+        step()
     torch.cuda.synchronize()
-    pga_s = time.perf_counter() - t0
-    geo = (tuple(lat.origin), tuple(lat.step_row), tuple(lat.step_col), lat.rows, lat.cols, sc.range_start,
-           sc.data_dr, sc.k)
-    entropy_autofocus(d, nav_t, w, ph, *geo, steps=2)
-    torch.cuda.synchronize()
-    res = entropy_autofocus(d, nav_t, w, ph, *geo, steps=20)
-    per_eval = res.history[-1][0] / res.evaluations
-    return {"pga_iters_per_s": len(records) / pga_s, "pga_iterations": len(records),
-            "entropy_evals_per_s": 1.0 / per_eval, "entropy_evaluations": res.evaluations,
-            "entropy_after": res.entropy,
-            "workload": "2048 pulses x 4096 bins, 1024^2 lattice; PGA: FFBP (leaf 64) + 12x12 target picks + "
-                        "estimate_update per iteration; entropy: forward + adjoint BP per L-BFGS evaluation"}
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    with Clocks(dev.index or 0) as clocks:
+        for i in range(steps):
+            flush.zero_()
+            ev0[i].record(stream)
+            step()
+            ev1[i].record(stream)
+        torch.cuda.synchronize()
+    ms = statistics.mean(ev0[i].elapsed_time(ev1[i]) for i in range(steps))
+    npix = lat.rows * lat.cols
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(npix, sample_pixels, replace=False)
+    ref = ora.backproject_points(sc.data, sc.position, lat.take(idx), sc.range_start, sc.data_dr, sc.k, sc.weight,
+                                 sc.phase, c128=True)[1]
+    est = out.reshape(-1)[torch.from_numpy(idx).to(dev)].cpu().numpy().astype(np.complex128)
+    return {"gpix_pulse_s": npix * cfg.pulses / (ms / 1e3) / 1e9, "ms": ms, "steps": steps,
+            "err_vs_fp64": float(np.linalg.norm(est - ref) / np.linalg.norm(ref)),
+            "err_sample": f"{sample_pixels} random pixels x all {cfg.pulses} pulses, complex L2 vs the FP64 oracle",
+            "pulse_split": core.lattice_pulse_split(lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols,
+                                                    "split"),
+            "workload": "c2 direct BP: 8192 pulses x 16384 bins -> 4096x4096 ground lattice @0.25 m, 10 GHz, "
+                        "300 MHz, 30 km near slant, split precision; L2 flushed before every step",
+            "synthesis_s": synth_s, "clocks": clocks.summary()}
 
 
 def run_autofocus(args, rank):
@@ -320,21 +373,17 @@ def run_autofocus(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args, rank):
+def batch_measure(dev, scenes_count, steps, warmup):
     """64 independent scenes of uneven size (half direct BP, half FFBP) as one CUDA graph of
     persistent work-queue launches, tile shapes from the autotuner; against the same scenes
-    formed one at a time through the single-scene entry points."""
-    if rank != 0:
-        return
+    formed one at a time through the single-scene entry points.  Returns the measurement dict."""
     import torch
 
-    from bp_project_gb300 import _native, autotune, build, core, scenes
+    from bp_project_gb300 import autotune, core, scenes
     from bp_project_gb300.batch import DirectScene, FFBPScene, SceneBatch
     from bp_project_gb300.gpu_backend import build_ffbp_plan
-    build.build()
-    dev = torch.device("cuda", 0)
     t0 = time.perf_counter()
-    cfgs = scenes.batch_configs(count=args.scenes)
+    cfgs = scenes.batch_configs(count=scenes_count)
     items = []
     for cfg, kind in cfgs:
         sc = scenes.synthesize(cfg, device=str(dev))
@@ -374,18 +423,18 @@ def run_batch(args, rank):
 
     batch = SceneBatch(items, blocks_per_sm=blocks)
     graph = batch.capture_graph()
-    for _ in range(max(args.warmup, 3) - 1):
+    for _ in range(max(warmup, 3) - 1):
         batch.replay()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(0) as clocks:
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             batch.replay()
         e1.record(stream)
         torch.cuda.synchronize()
-    batch_ms = e0.elapsed_time(e1) / args.steps
+    batch_ms = e0.elapsed_time(e1) / steps
 
     # The same scenes one at a time (single-scene entry points, default shapes), one pass.
     progs = [core.FFBPProgram(sc.plan.nodes(), sc.plan.crop_r, sc.plan.crop_u, mode="split", device=dev)
@@ -402,10 +451,11 @@ def run_batch(args, rank):
     sequential()
     torch.cuda.synchronize()
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s0.record(stream)
-    sequential()
-    s1.record(stream)
-    torch.cuda.synchronize()
+    with Clocks(dev.index or 0) as seq_clocks:
+        s0.record(stream)
+        sequential()
+        s1.record(stream)
+        torch.cuda.synchronize()
     seq_ms = s0.elapsed_time(s1)
     errs = [float((items[i].out - r).abs().norm() / r.abs().norm()) for i, r in default_ref.items()]
     for p in progs:
@@ -424,8 +474,8 @@ def run_batch(args, rank):
                 "max": float(v[-1])}
     line = {
         "metric": "batched scenes: Gpixel·pulses/s (direct-equivalent) and scenes/s", "value": px / (batch_ms / 1e3) / 1e9,
-        "unit": "Gpixel·pulses/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": batch_ms, "data": "synthetic", "dtype": "f32 (split precision)",
+        "unit": "Gpixel·pulses/s", "higher_is_better": True, "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": batch_ms, "data": "synthetic", "dtype": "f32 (split precision)",
         "config": {"workload": f"{len(items)} scenes: pulses U{{512..8192 step 512}}, side U{{256,512,1024,2048}} "
                                "@0.5 m, half direct BP / half FFBP (leaf 16), near slant U(3.5, 8) km, 4-16 "
                                "targets + 256 clutter, 9.6 GHz / 150 MHz",
@@ -439,6 +489,7 @@ def run_batch(args, rank):
         "autotune_blocks_per_sm": {"chosen": blocks, "ms": block_timings},
         "autotune_s": tune_s, "synthesis_s": synth_s,
         "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / batch_ms,
+        "sequential_clocks": seq_clocks.summary(),
         "scene_latency_ms": {"all": spread(lat_ms),
                              "direct": spread([t for t, k in zip(lat_ms, kinds) if k == "direct"]),
                              "ffbp": spread([t for t, k in zip(lat_ms, kinds) if k == "ffbp"]),
@@ -448,10 +499,21 @@ def run_batch(args, rank):
         "workspace_gb": batch.workspace_bytes / 1e9,
         "clocks": clocks.summary(),
         # graph replays bypass the C ABI's launch counter: count the graph's kernel nodes
-        "gpu_launches": args.steps * (batch.launch_count - 1),
+        "gpu_launches": steps * (batch.launch_count - 1),
     }
     batch.close()
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_batch(args, rank):
+    """The batch workload alone, as its own JSON line."""
+    if rank != 0:
+        return
+    import torch
+
+    from bp_project_gb300 import build
+    build.build()
+    print(json.dumps(batch_measure(torch.device("cuda", 0), args.scenes, args.steps, args.warmup)), flush=True)
 
 
 def main():
@@ -667,8 +729,22 @@ def main():
         })
         prog.close()
 
+    if rank == 0 and not args.no_c2:
+        from oracle import build as oracle_build
+        oracle_build.build()
+        extra["c2_direct"] = c2_direct(dev, steps=min(args.steps, 5), warmup=args.warmup)
+
     if rank == 0 and not args.no_autofocus:
-        extra["autofocus"] = autofocus_rates(dev)
+        from oracle import build as oracle_build
+        oracle_build.build()
+        extra["autofocus"] = autofocus_wall(dev)
+
+    if rank == 0 and not args.no_batch:
+        b = batch_measure(dev, args.scenes, steps=min(args.steps, 5), warmup=args.warmup)
+        keep = ("value", "unit", "ms_per_step", "steps", "scenes_per_s", "sequential_ms", "speedup_vs_sequential",
+                "scene_latency_ms", "graph", "gpu_launches", "clocks", "sequential_clocks",
+                "tuned_vs_default_shape_err_max", "autotune", "autotune_blocks_per_sm", "autotune_s", "synthesis_s")
+        extra["batch"] = {"workload": b["config"]["workload"], **{k_: b[k_] for k_ in keep}}
 
     if rank != 0:
         if world > 1:
