@@ -124,6 +124,7 @@ SIGNATURES = {
     "sarbp_target_contributions": ([_P, _I, _I, _P, _P, _I, _D, _D, _D, _P, _P], _I),
     "sarbp_fill_range_phase_lut": ([_I, _D, _D, _D, _P, _P], _I),
     "sarbp_direct_polar_lut": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _P, _P, _P], _I),
+    "sarbp_direct_polar_phase32": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _I, _P, _P], _I),
 }
 
 _lock = threading.Lock()

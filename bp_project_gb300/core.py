@@ -230,6 +230,18 @@ def direct_polar_lut(data, pos, weight, phase, grid: Grid, range_start, data_dr,
     return out
 
 
+def direct_polar_phase32(data, pos, weight, phase, grid: Grid, range_start, data_dr, k, wrapped=False, out=None):
+    """Mixed-geometry direct BP with the phase cast to FP32 for sincosf (gpu/precision_probe.cu:19-79);
+    ``wrapped`` reduces the FP64 phase with remainder(phase, 2 pi) first."""
+    p, s = check_pulses(data, pos, weight, phase)
+    if out is None:
+        out = torch.empty((grid.nr, grid.nu), dtype=torch.complex64, device=data.device)
+    g = grid.native()
+    nat.call("sarbp_direct_polar_phase32", _ptr(data), p, s, _ptr(pos), _ptr(weight), _ptr(phase), ctypes.byref(g),
+             float(range_start), float(data_dr), float(k), int(bool(wrapped)), _ptr(out), stream_handle())
+    return out
+
+
 def add_inplace(left, right):
     nat.call("sarbp_add_inplace", _ptr(left), _ptr(right), left.numel(), stream_handle())
     return left

@@ -704,4 +704,16 @@ int sarbp_direct_polar_lut(const float* data, int pulses, int samples, const dou
                                   reinterpret_cast<float2*>(out), (cudaStream_t)stream);
 }
 
+int sarbp_direct_polar_phase32(const float* data, int pulses, int samples, const double* pos, const double* weight,
+                               const double* phase, const sarbp_polar_grid* grid, double range_start, double data_dr,
+                               double k, int wrapped, float* out, void* stream) {
+    if (int st = check_pulses(data, pulses, samples, pos, weight, phase, data_dr, k)) return st;
+    if (int st = check_grid(grid)) return st;
+    if (!out) return fail(SARBP_ERR_TYPE, "out must not be NULL");
+    if (wrapped != 0 && wrapped != 1) return fail(SARBP_ERR_VALUE, "wrapped must be 0 or 1 (got %d)", wrapped);
+    const PulseInputs in = inputs_of(data, pulses, samples, pos, weight, phase, range_start, data_dr, k);
+    return launch_plain_polar_phase32(in, desc_of(*grid), wrapped != 0, reinterpret_cast<float2*>(out),
+                                      (cudaStream_t)stream);
+}
+
 }  // extern "C"

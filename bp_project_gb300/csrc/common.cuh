@@ -163,6 +163,8 @@ int launch_target_contrib(const PulseInputs& in, const double* xyz, int npts, fl
 int launch_fill_lut(int samples, double range_start, double data_dr, double k, float2* lut, cudaStream_t s);
 int launch_plain_polar_lut(const PulseInputs& in, const PolarDesc& g, const float2* lut, float2* out,
                            cudaStream_t s);
+int launch_plain_polar_phase32(const PulseInputs& in, const PolarDesc& g, bool wrapped, float2* out,
+                               cudaStream_t s);
 int launch_add(float2* left, const float2* right, int64_t n, cudaStream_t s);
 int launch_cast(const double2* in, float2* out, int64_t n, cudaStream_t s);
 int launch_crop(const float2* in, int src_nu, int r_begin, int u_begin, int nr, int nu, float2* out,

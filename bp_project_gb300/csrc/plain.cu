@@ -383,6 +383,47 @@ __global__ void __launch_bounds__(kThreads) plain_polar_lut_kernel(PulseInputs i
     if (active) out[(long long)wr * g.win_nu + wu] = make_float2(accr, acci);
 }
 
+// ---- FP32-sincos phase probes (gpu/precision_probe.cu:19-79) ----------------------
+// The mixed policy's FP64 geometry, sampling coordinate and phase k (d - r) + phase[n];
+// the finished phase is cast to FP32 and goes to the library sincosf (not the fast
+// intrinsic).  WRAP first reduces it with FP64 remainder(phi, 2 pi), which separates the
+// quantisation of a large angle in FP32 from the sincosf evaluation error.
+template <bool WRAP>
+__global__ void __launch_bounds__(kThreads) plain_polar_phase32_kernel(PulseInputs in, PolarDesc g,
+                                                                        float2* __restrict__ out) {
+    __shared__ PulseStage<SARBP_MIXED> st;
+    const long long p = (long long)blockIdx.x * kThreads + threadIdx.x;
+    const long long npix = (long long)g.win_nr * g.win_nu;
+    const bool active = p < npix;
+    const int wr = active ? (int)(p / g.win_nu) : 0;
+    const int wu = active ? (int)(p - (long long)wr * g.win_nu) : 0;
+    double x, y, r;
+    polar_point<double>(g, g.win_r0 + wr, g.win_u0 + wu, x, y, r);
+    float accr = 0.0f, acci = 0.0f;
+    for (int c0 = 0; c0 < in.pulses; c0 += kChunk) {
+        const int count = min(kChunk, in.pulses - c0);
+        __syncthreads();
+        stage_pulses<SARBP_MIXED>(st, in, c0, count);
+        __syncthreads();
+        if (!active) continue;
+        for (int t = 0; t < count; ++t) {
+            const double dx = x - st.pos[3 * t], dy = y - st.pos[3 * t + 1], dz = -st.pos[3 * t + 2];
+            const double d = sqrt(dx * dx + dy * dy + dz * dz);
+            float vr, vi;
+            sample1<SARBP_MIXED>(in.data + (size_t)(c0 + t) * in.samples, in.samples, (d - in.range_start) / in.data_dr,
+                                 vr, vi);
+            double phi = in.k * (d - r) + st.ph[t];
+            if (WRAP) phi = remainder(phi, 6.283185307179586476925286766559);
+            float sn, cs;
+            sincosf((float)phi, &sn, &cs);
+            const float a = st.w[t];
+            accr += a * (vr * cs - vi * sn);
+            acci += a * (vr * sn + vi * cs);
+        }
+    }
+    if (active) out[(long long)wr * g.win_nu + wu] = make_float2(accr, acci);
+}
+
 // ---- elementwise ----------------------------------------------------------------
 __global__ void add_kernel(float2* __restrict__ left, const float2* __restrict__ right, int64_t n) {
     const int64_t p = (int64_t)blockIdx.x * kThreads + threadIdx.x;
@@ -520,6 +561,17 @@ int launch_plain_polar_lut(const PulseInputs& in, const PolarDesc& g, const floa
     plain_polar_lut_kernel<<<grid_blocks(npix, kThreads), kThreads, 0, s>>>(in, g, lut, out);
     note_launches(1);
     return check_launch("direct_polar_lut");
+}
+
+int launch_plain_polar_phase32(const PulseInputs& in, const PolarDesc& g, bool wrapped, float2* out,
+                               cudaStream_t s) {
+    const long long npix = (long long)g.win_nr * g.win_nu;
+    if (wrapped)
+        plain_polar_phase32_kernel<true><<<grid_blocks(npix, kThreads), kThreads, 0, s>>>(in, g, out);
+    else
+        plain_polar_phase32_kernel<false><<<grid_blocks(npix, kThreads), kThreads, 0, s>>>(in, g, out);
+    note_launches(1);
+    return check_launch("direct_polar_phase32");
 }
 
 int launch_add(float2* left, const float2* right, int64_t n, cudaStream_t s) {

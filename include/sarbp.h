@@ -358,6 +358,17 @@ int sarbp_direct_polar_lut(const float* data, int pulses, int samples, const dou
                            double range_start, double data_dr, double k, const float* lut, float* out,
                            void* stream);
 
+/* ---- FP32-sincos phase probes (gpu/precision_probe.cu:19-79) ----------------
+ * Replaces direct_chunk_mixed_phase32 (wrapped = 0) and
+ * direct_chunk_mixed_phase32_wrapped (wrapped = 1): the mixed policy's FP64
+ * geometry, sampling coordinate and phase k (d - r) + phase[n], with the phase
+ * cast to FP32 for the library sincosf; wrapped = 1 first reduces it with FP64
+ * remainder(phase, 2 pi).  All pulses in one launch; out complex64 [nr, nu]. */
+int sarbp_direct_polar_phase32(const float* data, int pulses, int samples, const double* pos,
+                               const double* weight, const double* phase, const sarbp_polar_grid* grid,
+                               double range_start, double data_dr, double k, int wrapped, float* out,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

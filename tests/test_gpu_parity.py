@@ -417,3 +417,25 @@ def test_direct_polar_lut_probe(golden, lib):
     lut = core.fill_range_phase_lut(g[p + "data"].shape[1], range_start, data_dr, k)
     out = core.direct_polar_lut(*args, plan.grid(), range_start, data_dr, k, lut)
     assert rel_err(g[p + "direct"], out.cpu().numpy()) <= 1e-4
+
+
+@pytest.mark.parametrize("case", [0, 1])
+def test_direct_polar_phase32_probes(golden, lib, case):
+    """The FP32-sincos phase probes (gpu/precision_probe.cu:19-79) on the operator-validation recipe,
+    against the reference's own FP64 direct BP: both within 1e-6 (a numpy restatement of the probe
+    arithmetic gives 1.9e-7 unwrapped, 8e-8 wrapped, on these cases), the same peak pixel, and the
+    FP64 remainder(phase, 2 pi) no worse than the plain cast."""
+    from bp_project_gb300 import core
+    g, p, plan, range_start, data_dr, fc, k, side, extent = _op_case(golden, case)
+    args = (_dev(g[p + "data"], torch.complex64), _dev(g[p + "position"], torch.float64),
+            _dev(g[p + "weight"], torch.float64), _dev(g[p + "phase"], torch.float64))
+    ref = g[p + "direct"]
+    errs = {}
+    for wrapped in (False, True):
+        out = core.direct_polar_phase32(*args, plan.grid(), range_start, data_dr, k, wrapped=wrapped).cpu().numpy()
+        assert np.isfinite(out).all()
+        errs[wrapped] = rel_err(ref, out)
+        assert errs[wrapped] <= 1e-6, (wrapped, errs[wrapped])
+        assert (np.unravel_index(np.abs(out).argmax(), out.shape)
+                == np.unravel_index(np.abs(ref).argmax(), ref.shape))
+    assert errs[True] <= 1.2 * errs[False] + 1e-8, errs
