@@ -17,6 +17,12 @@ lattice, polar grid and points, FFBP, evaluation, target contributions, the
 LUT probe, adjoint, range compression, I/Q decode, phase-history filter).
 Prints one JSON line with event timings (not for benchmarking under a
 profiler: bench.py is the benchmark).
+
+As in the reference's profiling target (fast_bp/resident_profile_target.py:83-99),
+``--warmups`` runs untimed repetitions first, and the measured repetitions run
+between cudaProfilerStart and cudaProfilerStop inside an NVTX range named
+``sarbp_profile``, so that a profiler can capture only them
+(``ncu --profile-from-start off`` or an NVTX filter).
 """
 from __future__ import annotations
 
@@ -88,6 +94,7 @@ def main(argv=None):
     ap.add_argument("--side", type=int, default=None, help="scale the ground image to side x side pixels")
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--mode", default="split")
+    ap.add_argument("--warmups", type=int, default=0, help="untimed repetitions before the profiled range")
     args = ap.parse_args(argv)
     build.build()
     torch.cuda.set_device(0)
@@ -165,13 +172,27 @@ def main(argv=None):
             core.evaluate_lattice(polar, grid, lat.origin, lat.step_row, lat.step_col, lat.rows, lat.cols, scene.k,
                                   out=ground)
         units = lat.rows * lat.cols * cfg.pulses
-    for _ in range(args.reps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
+    for _ in range(args.warmups):
         run()
-        b.record()
-        torch.cuda.synchronize()
-        times.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()  # cudaProfilerStart: the capture range of --profile-from-start off
+    nvtx = True
+    try:
+        torch.cuda.nvtx.range_push("sarbp_profile")
+    except (AttributeError, RuntimeError):  # torch built without NVTX: the profiler API range remains
+        nvtx = False
+    try:
+        for _ in range(args.reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            run()
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+    finally:
+        if nvtx:
+            torch.cuda.nvtx.range_pop()
+        torch.cuda.profiler.stop()
     print(json.dumps({"workload": args.workload, "config": cfg.name, "pulses": cfg.pulses,
                       "image": [lat.rows, lat.cols], "mode": args.mode, "ms": times,
                       "gpix_pulse_per_s": [units / (t / 1e3) / 1e9 for t in times]}), flush=True)
