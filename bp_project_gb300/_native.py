@@ -100,6 +100,7 @@ SIGNATURES = {
     "sarbp_batch_bind": ([_P, _P, _Z, _P], _I),
     "sarbp_batch_execute": ([_P, _P], _I),
     "sarbp_batch_set_trace": ([_P, _P], _I),
+    "sarbp_batch_set_concurrent": ([_P, _I], _I),
     "sarbp_rc_prepare": ([_P, _I, _I, _I, _P, _P], _I),
     "sarbp_decode_iq": ([_P, _I, _I64, _I, _I, _P, _P], _I),
     "sarbp_rc_filter": ([_P, _P, _I, _I, _I, _P, _P], _I),
@@ -125,6 +126,7 @@ SIGNATURES = {
     "sarbp_fill_range_phase_lut": ([_I, _D, _D, _D, _P, _P], _I),
     "sarbp_direct_polar_lut": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _P, _P, _P], _I),
     "sarbp_direct_polar_phase32": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _I, _P, _P], _I),
+    "sarbp_fp32_peak": ([_I, _I, ctypes.POINTER(_D)], _I),
 }
 
 _lock = threading.Lock()

@@ -4,7 +4,8 @@ The tunables are the tile shape (``tile_lc``: 1 << lc columns by 1024 >> lc rows
 the reference's equivalent knob is the 256-thread block over a flat pixel range)
 and the pulses staged per chunk (``chunk_pulses``, the reference's
 ``--chunk-pulses``, gpu_baseline.py:413), plus the CTAs per SM of the persistent
-batch launch.  For a scene class (image side, pixel spacing, range geometry)
+batch launch and whether the batch's FFBP chain runs on its own stream beside the
+direct queue.  For a scene class (image side, pixel spacing, range geometry)
 ``tune_direct`` times every candidate on a representative scene through
 ``SceneBatch`` (CUDA events, after a warm-up) and keeps the fastest; results are
 cached per device and class in a JSON file.
@@ -31,8 +32,8 @@ def _key(scene: DirectScene, device) -> str:
     return f"{name}|direct|side{max(scene.rows, scene.cols)}|dx{spacing:.3g}|dr{scene.data_dr:.4g}"
 
 
-def _time(scenes, blocks_per_sm, reps):
-    batch = SceneBatch(scenes, blocks_per_sm=blocks_per_sm)
+def _time(scenes, blocks_per_sm, reps, concurrent=False):
+    batch = SceneBatch(scenes, blocks_per_sm=blocks_per_sm, concurrent=concurrent)
     try:
         batch.execute()
         torch.cuda.synchronize()
@@ -78,10 +79,15 @@ def apply(scenes, choices):
             sc.tile_lc, sc.chunk_pulses = lc, ch
 
 
-def tune_blocks(scenes, blocks=BLOCKS_PER_SM, reps=1):
-    """CTAs per SM of the persistent launch for the whole batch (timed on the batch itself)."""
+def tune_blocks(scenes, blocks=BLOCKS_PER_SM, reps=1, concurrent=(False, True)):
+    """CTAs per SM of the persistent direct launch, and whether the FFBP chain runs on its own stream
+    beside it, for the whole batch (timed on the batch itself).  Returns ((blocks_per_sm, concurrent),
+    {"blocks,concurrent": ms})."""
     timings = {}
-    for bps in blocks:
-        fresh = [type(sc)(**{**sc.__dict__, "out": None}) for sc in scenes]
-        timings[bps] = _time(fresh, bps, reps)
-    return min(timings, key=timings.get), timings
+    for conc in concurrent:
+        for bps in blocks:
+            fresh = [type(sc)(**{**sc.__dict__, "out": None}) for sc in scenes]
+            timings[f"{bps},{int(conc)}"] = _time(fresh, bps, reps, conc)
+    best = min(timings, key=timings.get)
+    bps, conc = best.split(",")
+    return (int(bps), bool(int(conc))), timings

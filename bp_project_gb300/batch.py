@@ -7,7 +7,10 @@ a second one, and the FFBP merges as one persistent launch per tree height
 across all scenes.
 ``execute`` only enqueues work on the current stream (no allocation, no
 synchronisation), so the whole batch can be captured in one CUDA graph
-(``capture_graph`` / ``replay``), like ``ResidentProgram``.
+(``capture_graph`` / ``replay``), like ``ResidentProgram``.  With
+``concurrent=True`` the FFBP chain runs on a stream of the batch's own, forked
+from and joined back to the current stream, beside the direct queue: the
+latency-bound merges and the issue-bound direct tiles then share the SMs.
 
 The reference images one scene at a time; its ``BatchedResidentProgram``
 (fast_bp/batched_resident_backend.py:23-157) batches the levels of one tree.
@@ -62,7 +65,7 @@ class FFBPScene:
 class SceneBatch:
     """A fixed set of scenes formed by one schedule (inputs and outputs bound at construction)."""
 
-    def __init__(self, scenes, blocks_per_sm=0, device=None):
+    def __init__(self, scenes, blocks_per_sm=0, device=None, concurrent=False):
         if not scenes:
             raise ValueError("a batch needs at least one scene")
         self.scenes = list(scenes)
@@ -105,6 +108,8 @@ class SceneBatch:
         self.workspace = torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8, device=dev)
         nat.check(lib.sarbp_batch_bind(handle, core._ptr(self.workspace), self.workspace.numel(),
                                        core.stream_handle()), "batch_bind")
+        nat.check(lib.sarbp_batch_set_concurrent(handle, int(bool(concurrent))), "batch_set_concurrent")
+        self.concurrent = bool(concurrent)
         self.launch_count = int(lib.sarbp_batch_launch_count(handle))
         vals = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()]
         nat.check(lib.sarbp_batch_info(handle, *[ctypes.byref(v) for v in vals]), "batch_info")

@@ -242,6 +242,14 @@ def direct_polar_phase32(data, pos, weight, phase, grid: Grid, range_start, data
     return out
 
 
+def fp32_peak_tflops(packed: bool = False, iters: int = 16384) -> float:
+    """Measured FP32 issue rate of the current GPU in TFLOP/s (FMA = 2): eight independent FMA
+    chains per thread at full occupancy, scalar or packed f32x2 (sarbp_fp32_peak)."""
+    out = ctypes.c_double()
+    nat.call("sarbp_fp32_peak", int(bool(packed)), int(iters), ctypes.byref(out))
+    return float(out.value)
+
+
 def add_inplace(left, right):
     nat.call("sarbp_add_inplace", _ptr(left), _ptr(right), left.numel(), stream_handle())
     return left

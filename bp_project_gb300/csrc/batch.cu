@@ -43,6 +43,18 @@ struct sarbp_batch {
     void* bound = nullptr;
     unsigned long long* trace = nullptr;  // per-scene completion times (ns) + the start time, or none
     int launches = 0;
+    // Concurrent mode: the FFBP chain (prologues, leaves, merges) runs on `side`, forked from and
+    // joined back to the caller's stream with events, beside the direct queue on the caller's
+    // stream.  A graph captured on the caller's stream records both branches.
+    bool concurrent = false;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+
+    ~sarbp_batch() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
+    }
 };
 
 namespace {
@@ -307,6 +319,19 @@ int sarbp_batch_bind(sarbp_batch* batch, void* workspace, size_t workspace_bytes
     return SARBP_OK;
 }
 
+int sarbp_batch_set_concurrent(sarbp_batch* batch, int on) {
+    if (!batch) return fail(SARBP_ERR_TYPE, "batch must not be NULL");
+    if (on != 0 && on != 1) return fail(SARBP_ERR_VALUE, "on must be 0 or 1 (got %d)", on);
+    if (on && !batch->side) {
+        cudaError_t e = cudaStreamCreateWithFlags(&batch->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&batch->fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&batch->join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "batch side stream: %s", cudaGetErrorString(e));
+    }
+    batch->concurrent = on != 0;
+    return SARBP_OK;
+}
+
 int sarbp_batch_execute(const sarbp_batch* batch, void* stream) {
     if (!batch) return fail(SARBP_ERR_TYPE, "batch must not be NULL");
     if (!batch->bound) return fail(SARBP_ERR_PLAN, "sarbp_batch_bind must succeed before execute");
@@ -327,23 +352,37 @@ int sarbp_batch_execute(const sarbp_batch* batch, void* stream) {
     if (trace && e == cudaSuccess) e = cudaMemsetAsync(trace, 0, sizeof(unsigned long long) * batch->n_scenes, s);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "batch counters: %s", cudaGetErrorString(e));
     int st = trace ? launch_split_batch_trace_start(trace + batch->n_scenes, s) : SARBP_OK;
-    if (batch->ffbp_scenes)
+    // The FFBP chain goes to the side stream when the batch runs concurrently and has both kinds.
+    const bool fork = batch->concurrent && batch->ffbp_scenes && batch->direct_scenes;
+    cudaStream_t fs = fork ? batch->side : s;
+    if (st == SARBP_OK && fork) {
+        e = cudaEventRecord(batch->fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(fs, batch->fork, 0);
+        if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "batch fork: %s", cudaGetErrorString(e));
+    }
+    if (st == SARBP_OK && batch->ffbp_scenes)
         st = launch_split_batch_prologue(scenes, nodes, (int)batch->nodes.size(), batch->max_dim, leaves,
                                          (int)batch->leaves.size(), merge_items, (int)batch->merge_items.size(),
-                                         tables, precs, crecs, arena, s);
+                                         tables, precs, crecs, arena, fs);
     const int n_leaf = (int)batch->bp_items.size() - batch->n_direct;
     if (st == SARBP_OK)
         st = launch_split_batch_direct(scenes, bp_items, batch->n_direct, counters, batch->bp_blocks,
                                        batch->direct_smem, trace, s);
     if (st == SARBP_OK)
         st = launch_split_batch_leaves(scenes, nodes, bp_items + batch->n_direct, n_leaf, tables, precs, arena,
-                                       counters + 1, batch->leaf_blocks, batch->leaf_smem, trace, s);
+                                       counters + 1, batch->leaf_blocks, batch->leaf_smem, trace, fs);
     const size_t crec_size = split_ffbp_child_record_bytes();
     for (int h = 1; h <= batch->max_height && st == SARBP_OK; ++h) {
         const int first = batch->level_begin[h - 1], count = batch->level_count[h - 1];
         st = launch_split_batch_merges(scenes, nodes, merge_items + first, count, tables,
                                        crecs + 2 * (size_t)first * crec_size, arena, counters + 1 + h,
-                                       std::min(batch->merge_blocks, std::max(1, count)), trace, s);
+                                       std::min(batch->merge_blocks, std::max(1, count)), trace, fs);
+    }
+    if (fork) {
+        // Join even after a failed launch, so that a stream capture is never left forked.
+        e = cudaEventRecord(batch->join, fs);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, batch->join, 0);
+        if (e != cudaSuccess && st == SARBP_OK) st = fail(SARBP_ERR_CUDA, "batch join: %s", cudaGetErrorString(e));
     }
     return st;
 }

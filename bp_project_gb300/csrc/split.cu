@@ -130,6 +130,9 @@ struct Job {
     int p0, p1;
 };
 
+// (v, v): an operand of the packed FP32 (f32x2) instructions.
+__device__ __forceinline__ float2 pair(float v) { return make_float2(v, v); }
+
 // ---- block reductions (256 threads) ---------------------------------------------
 template <int N>
 __device__ __forceinline__ void block_max(TileShared& S, float v[N]) {
@@ -577,6 +580,82 @@ __device__ __forceinline__ void fast_chunk(const SplitParams& P, const Rec* __re
     }
 }
 
+// fast_chunk for 2-D demodulated tiles (polar grids) with the thread's pixels k = 2h, 2h + 1
+// as packed FP32 (f32x2) pairs through the range, fraction, window-index and phase steps; the
+// complex cubic evaluates (re, im) as one pair and the accumulation stays scalar.  Every half
+// rounds like fast_chunk's scalar operation, and the chain carries -L, -q2, -e0 and -eps
+// (negation is exact), so the image is fast_chunk<false, true>'s bit for bit:
+//   -L = (-u) . delta,  -q2 = (-L)^2 - d2,  2L + 2R = -2 (-L) + 2R,  -e0 = -q2 B,
+//   -eps = (-e0)^2 B + (-e0),  qp = ((-L) + (-eps)) (-1/dr) + Fm,  sm = -K (-eps) + Phi + ...
+__device__ __forceinline__ void polar_chunk(const SplitParams& P, const Rec* __restrict__ rec,
+                                            const float4* __restrict__ win, int chn, Pix px[kPX]) {
+    static_assert(kPX == 4, "two pixel pairs per thread");
+    const float2 ninv = pair(-P.inv_drf), nKf = pair(-P.Kf), mone = pair(-1.0f), mtwo = pair(-2.0f);
+    const float2 magic = pair(kMagic), nmagic = pair(-kMagic), twopi = pair(kTwoPiF);
+    float2 dx[2], dy[2], dxh[2], dyh[2], dxl[2], dyl[2], nd2[2], psi[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const Pix &a = px[2 * h], &b = px[2 * h + 1];
+        dx[h] = make_float2(a.dx, b.dx);
+        dy[h] = make_float2(a.dy, b.dy);
+        dxh[h] = make_float2(a.dxh, b.dxh);
+        dyh[h] = make_float2(a.dyh, b.dyh);
+        dxl[h] = make_float2(a.dxl, b.dxl);
+        dyl[h] = make_float2(a.dyl, b.dyl);
+        nd2[h] = make_float2(-a.d2, -b.d2);
+        psi[h] = make_float2(a.psi, b.psi);
+    }
+#pragma unroll 1
+    for (int nl = 0; nl < chn; ++nl) {
+        const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c;
+        const int bias = __float_as_int(rc.y);
+        const unsigned last = (unsigned)__float_as_int(rc.w);
+        const float4* wrow = win + 2 * __float_as_int(rc.z);
+        const float2 nux = pair(-rb.x), nuy = pair(-rb.y), twoR = pair(rb.z), fm = pair(rb.w);
+        const float2 Wx = pair(ra.x), Wy = pair(ra.y), Wlx = pair(ra.z), Wly = pair(ra.w), phi = pair(rc.x);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float2 nL = __ffma2_rn(nux, dx[h], __fmul2_rn(nuy, dy[h]));
+            const float2 nq2 = __ffma2_rn(nL, nL, nd2[h]);
+            const float2 den = __ffma2_rn(mtwo, nL, twoR);
+            const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+            const float2 ne0 = __fmul2_rn(nq2, B);
+            const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);
+            const float2 qp = __ffma2_rn(__fadd2_rn(nL, neps), ninv, fm);
+            const float2 tq = __fadd2_rn(qp, magic);
+            const float2 sv = __ffma2_rn(__fadd2_rn(tq, nmagic), mone, qp);
+            const float2 tb = __ffma2_rn(Wx, dxh[h], __fmul2_rn(Wy, dyh[h]));  // exact
+            float2 sm = __ffma2_rn(nKf, neps, phi);
+            sm = __ffma2_rn(Wx, dxl[h], sm);
+            sm = __ffma2_rn(Wy, dyl[h], sm);
+            sm = __ffma2_rn(Wlx, dx[h], sm);
+            sm = __ffma2_rn(Wly, dy[h], sm);
+            sm = __fadd2_rn(sm, psi[h]);
+            // The reduced large term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps <= 1 + envelope / 2
+            // turns, so the angle stays within +-40 rad, which the hardware sin/cos reduce themselves.
+            const float2 rtb = __fadd2_rn(__fadd2_rn(tb, magic), nmagic);
+            const float2 ang = __fmul2_rn(__fadd2_rn(__ffma2_rn(rtb, mone, tb), sm), twopi);
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                Pix& q = px[2 * h + c];
+                const unsigned j = min((unsigned)(__float_as_int(c ? tq.y : tq.x) - bias), last);
+                const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+                const float2 ss = pair(c ? sv.y : sv.x);
+                const float2 v = __ffma2_rn(
+                    __ffma2_rn(__ffma2_rn(make_float2(c23.z, c23.w), ss, make_float2(c23.x, c23.y)), ss,
+                               make_float2(c01.z, c01.w)),
+                    ss, make_float2(c01.x, c01.y));
+                float sn, cs;
+                __sincosf(c ? ang.y : ang.x, &sn, &cs);
+                q.ar = fmaf(v.x, cs, q.ar);
+                q.ar = fmaf(-v.y, sn, q.ar);
+                q.ai = fmaf(v.x, sn, q.ai);
+                q.ai = fmaf(v.y, cs, q.ai);
+            }
+        }
+    }
+}
+
 // ---- two-float arithmetic (unevaluated sums hi + lo of two FP32 numbers) ----------------
 //
 // Error-free transformations (Knuth's two-sum, the FMA form of Dekker's product) give about
@@ -931,7 +1010,12 @@ struct ForwardBody {
     const SplitParams& P;
     const TileShared& S;
     Pix* px;
-    __device__ void fast(const Rec* rec, const float4* win, int nfit, int) { fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px); }
+    __device__ void fast(const Rec* rec, const float4* win, int nfit, int) {
+        if (!HAS_Z && DEMOD)
+            polar_chunk(P, rec, win, nfit, px);
+        else
+            fast_chunk<HAS_Z, DEMOD>(P, rec, win, nfit, px);
+    }
     __device__ void slow(int c0, int nslow, const SlowRec* srec) {
 #pragma unroll
         for (int k = 0; k < kPX; ++k) {
@@ -958,7 +1042,6 @@ __device__ void pulse_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 // r0 = frac(Phi + W . delta) from the exact hi products; its other pixels are kc = -2..1
 // steps of m rows away, L = L0 + kc (m u . s_row) and phase r0 + kc frac(m W . s_row).
 // Per pixel-pulse this leaves the eps term, the window gather and the rotation.
-__device__ __forceinline__ float2 pair(float v) { return make_float2(v, v); }
 
 // The forward's per-pixel geometry runs on packed FP32 (f32x2): pixels k = 2h and 2h + 1 of
 // a thread form one float2 lane pair through the range, fraction, index and angle steps, so
@@ -1990,18 +2073,148 @@ __device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const
     return make_float2(vr * cs - vi * sn, vr * sn + vi * cs);
 }
 
+// Both child records of a merge tile, each field a (child 0, child 1) pair, so that the two
+// children's coordinate, weight and phase chains run as packed FP32 (f32x2) instructions.
+// Negated copies stand in for the scalar code's subtractions (negation is exact), so every
+// value equals child_value's bit for bit.
+struct __align__(16) ChildPair {
+    float2 nbx, nby;   // -u.x, -u.y
+    float2 bz, bw;     // 2 RR, frac(Qr) - 1/2
+    float2 ncy, ncz;   // -h.x, -h.y
+    float2 cz, cw;     // h.y, 2 G
+    float2 dx, dy;     // G, frac(Qu) - 1/2
+    float2 nisr, isu;  // -1/sdr, 1/sdu
+    float2 ax, ay;     // W_hi.x, W_hi.y
+    float2 az, aw;     // W_lo.x, W_lo.y
+    float2 cx, pad;    // Phi
+    int2 ir0, iu0, snr, snu;
+    const float2* img[2];
+};
+
+// Thread c in {0, 1} moves child c's record into the pair layout.
+__device__ __forceinline__ void child_pair_store(const ChildRec& R, int c, ChildPair& P) {
+    reinterpret_cast<float*>(&P.nbx)[c] = -R.b.x;
+    reinterpret_cast<float*>(&P.nby)[c] = -R.b.y;
+    reinterpret_cast<float*>(&P.bz)[c] = R.b.z;
+    reinterpret_cast<float*>(&P.bw)[c] = R.b.w;
+    reinterpret_cast<float*>(&P.ncy)[c] = -R.c.y;
+    reinterpret_cast<float*>(&P.ncz)[c] = -R.c.z;
+    reinterpret_cast<float*>(&P.cz)[c] = R.c.z;
+    reinterpret_cast<float*>(&P.cw)[c] = R.c.w;
+    reinterpret_cast<float*>(&P.dx)[c] = R.d.x;
+    reinterpret_cast<float*>(&P.dy)[c] = R.d.y;
+    reinterpret_cast<float*>(&P.nisr)[c] = -R.inv_sdr;
+    reinterpret_cast<float*>(&P.isu)[c] = R.inv_sdu;
+    reinterpret_cast<float*>(&P.ax)[c] = R.a.x;
+    reinterpret_cast<float*>(&P.ay)[c] = R.a.y;
+    reinterpret_cast<float*>(&P.az)[c] = R.a.z;
+    reinterpret_cast<float*>(&P.aw)[c] = R.a.w;
+    reinterpret_cast<float*>(&P.cx)[c] = R.c.x;
+    reinterpret_cast<float*>(&P.pad)[c] = 0.0f;
+    reinterpret_cast<int*>(&P.ir0)[c] = R.ir0;
+    reinterpret_cast<int*>(&P.iu0)[c] = R.iu0;
+    reinterpret_cast<int*>(&P.snr)[c] = R.snr;
+    reinterpret_cast<int*>(&P.snu)[c] = R.snu;
+    P.img[c] = R.img;
+}
+
+// 4x4 Lagrange stencil of one child at bin (ir, iu) with weights wr (range) and wu (angle);
+// (re, im) run as one f32x2 pair.
+__device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, int snu, int ir, int iu,
+                                                const float wr[4], const float wu[4]) {
+    const float2* base = img + (size_t)(ir - 1) * snu + (iu - 1);
+    float2 v = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float2* row = base + (size_t)a * snu;
+        const float2 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2), x3 = __ldg(row + 3);
+        float2 r = __fmul2_rn(pair(wu[0]), x0);
+        r = __ffma2_rn(pair(wu[1]), x1, r);
+        r = __ffma2_rn(pair(wu[2]), x2, r);
+        r = __ffma2_rn(pair(wu[3]), x3, r);
+        v = __ffma2_rn(pair(wr[a]), r, v);
+    }
+    return v;
+}
+
+// The parent pixel q from both children: child_value(C0, q) + child_value(C1, q) (each child
+// rounded to complex64, then the FP32 add) with the two children's coordinate and phase chains
+// as packed FP32 pairs.  Both children's phase, sin/cos and bin indices come first, then each
+// child's Lagrange weights just before its stencil, which keeps the live state small enough for
+// two pixels in flight at 40 registers.
+__device__ __forceinline__ float2 child_pair_value(float Kf, const ChildPair& C, const Pix& q) {
+    const float2 dx = pair(q.dx), dy = pair(q.dy), nd2 = pair(-q.d2), mone = pair(-1.0f);
+    const float2 magic = pair(kMagic), nmagic = pair(-kMagic);
+    const float2 nL = __ffma2_rn(C.nbx, dx, __fmul2_rn(C.nby, dy));
+    const float2 nq2 = __ffma2_rn(nL, nL, nd2);
+    const float2 den = __ffma2_rn(pair(-2.0f), nL, C.bz);
+    const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    const float2 ne0 = __fmul2_rn(nq2, B);
+    const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);
+    // Phase (turns) first, so that the pixel's offsets die before the stencils.
+    const float2 tb = __ffma2_rn(C.ax, pair(q.dxh), __fmul2_rn(C.ay, pair(q.dyh)));
+    float2 sm = __ffma2_rn(pair(-Kf), neps, C.cx);
+    sm = __ffma2_rn(C.ax, pair(q.dxl), sm);
+    sm = __ffma2_rn(C.ay, pair(q.dyl), sm);
+    sm = __ffma2_rn(C.az, dx, sm);
+    sm = __ffma2_rn(C.aw, dy, sm);
+    const float2 rtb = __fadd2_rn(__fadd2_rn(tb, magic), nmagic);
+    const float2 tot = __fadd2_rn(__ffma2_rn(rtb, mone, tb), __fadd2_rn(sm, pair(q.psi)));
+    const float2 rtot = __fadd2_rn(__fadd2_rn(tot, magic), nmagic);
+    const float2 ang = __fmul2_rn(__ffma2_rn(rtot, mone, tot), pair(kTwoPiF));
+    float sn0, cs0, sn1, cs1;
+    __sincosf(ang.x, &sn0, &cs0);
+    __sincosf(ang.y, &sn1, &cs1);
+    const float2 qr = __ffma2_rn(__fadd2_rn(nL, neps), C.nisr, C.bw);
+    const float2 tr = __fadd2_rn(qr, magic);
+    const float2 sr = __ffma2_rn(__fadd2_rn(tr, nmagic), mone, qr);
+    const float2 nLh = __ffma2_rn(C.ncy, dx, __fmul2_rn(C.ncz, dy));
+    const float2 nq2h = __ffma2_rn(nLh, nLh, nd2);
+    const float2 denh = __ffma2_rn(pair(-2.0f), nLh, C.cw);
+    const float2 Bh = make_float2(rcp_approx(denh.x), rcp_approx(denh.y));
+    const float2 neh = __fmul2_rn(nq2h, Bh);
+    const float2 ndG = __fadd2_rn(nLh, __ffma2_rn(__fmul2_rn(neh, neh), Bh, neh));
+    const float2 gp = __ffma2_rn(ndG, mone, C.dx);
+    const float2 num = __ffma2_rn(C.cz, ndG, dy);
+    const float2 duu = __fmul2_rn(num, make_float2(rcp_approx(gp.x), rcp_approx(gp.y)));
+    const float2 qu = __ffma2_rn(duu, C.isu, C.dy);
+    const float2 tu = __fadd2_rn(qu, magic);
+    const float2 su = __ffma2_rn(__fadd2_rn(tu, nmagic), mone, qu);
+    const int ir0 = C.ir0.x + (__float_as_int(tr.x) - kMagicBits), ir1 = C.ir0.y + (__float_as_int(tr.y) - kMagicBits);
+    const int iu0 = C.iu0.x + (__float_as_int(tu.x) - kMagicBits), iu1 = C.iu0.y + (__float_as_int(tu.y) - kMagicBits);
+    const bool ok0 = ir0 >= 1 && ir0 <= C.snr.x - 3 && iu0 >= 1 && iu0 <= C.snu.x - 3 && gp.x > 0.0f;
+    const bool ok1 = ir1 >= 1 && ir1 <= C.snr.y - 3 && iu1 >= 1 && iu1 <= C.snu.y - 3 && gp.y > 0.0f;
+    float2 v0 = make_float2(0.0f, 0.0f), v1 = v0;
+    if (ok0) {
+        float wr[4], wu[4];
+        lagrange_centred(sr.x, wr);
+        lagrange_centred(su.x, wu);
+        v0 = child_stencil(C.img[0], C.snu.x, ir0, iu0, wr, wu);
+    }
+    if (ok1) {
+        float wr[4], wu[4];
+        lagrange_centred(sr.y, wr);
+        lagrange_centred(su.y, wu);
+        v1 = child_stencil(C.img[1], C.snu.y, ir1, iu1, wr, wu);
+    }
+    // (vr cs - vi sn, vr sn + vi cs) per child, then the complex64 sum.
+    const float2 o0 = __ffma2_rn(pair(v0.x), make_float2(cs0, sn0), __fmul2_rn(pair(v0.y), make_float2(-sn0, cs0)));
+    const float2 o1 = __ffma2_rn(pair(v1.x), make_float2(cs1, sn1), __fmul2_rn(pair(v1.y), make_float2(-sn1, cs1)));
+    return __fadd2_rn(o0, o1);
+}
+
 // One merge tile: both children regridded onto the parent tile, each rounded to complex64,
 // then added (the reference's rounding points).  crec points at the tile's two child records.
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
-                                           ChildRec* C, float2* __restrict__ arena, float2* root_out, int root,
+                                           ChildPair& C, float2* __restrict__ arena, float2* root_out, int root,
                                            TileShared& S, char* smem) {
     Job J;
     J.g = nodes[it.node];
     J.lc = J.g.tile_lc;
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
-    if (threadIdx.x < 2) C[threadIdx.x] = crec[threadIdx.x];
+    if (threadIdx.x < 2) child_pair_store(crec[threadIdx.x], threadIdx.x, C);
     TabF& T = *reinterpret_cast<TabF*>(smem);
     setup_polar_tab(J, S, T, tables);
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
@@ -2013,11 +2226,9 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
         const int p = threadIdx.x + kThreads * k;
         const int row = p >> J.lc, col = p & (cols_t - 1);
         const Pix v = tab_pixel(T, row, col);
-        const float2 a = child_value(Kf, C[0], v);
-        const float2 b = child_value(Kf, C[1], v);
+        const float2 m = child_pair_value(Kf, C, v);
         const int wr = J.tile_r + row, wu = J.tile_u + col;
-        if (wr < J.g.win_nr && wu < J.g.win_nu)
-            dst[(long long)wr * J.g.out_stride + wu] = make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+        if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m;
     }
 }
 
@@ -2029,7 +2240,7 @@ __global__ void __launch_bounds__(kThreads, 6) split_merge_kernel(SplitParams P,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ ChildRec C[2];
+    __shared__ ChildPair C;
     merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, S,
                smem);
 }
@@ -2441,7 +2652,7 @@ __global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchSce
                                                                   unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ ChildRec C[2];
+    __shared__ ChildPair C;
     __shared__ int s_item;
     for (;;) {
         const int idx = next_item(counter, s_item);

@@ -240,6 +240,12 @@ int sarbp_batch_execute(const sarbp_batch* batch, void* stream);
  * trace[i] - trace[n_scenes] is scene i's latency within the batch.  NULL switches tracing off (a
  * captured graph keeps the setting it was captured with). */
 int sarbp_batch_set_trace(sarbp_batch* batch, unsigned long long* trace);
+/* on = 1: execute runs the FFBP scenes' chain (prologues, leaf queue, merge levels) on a stream of
+ * the batch's own, forked from and joined back to the execute stream with events, so that it runs
+ * beside the direct-scene queue and the GPU's CTA slots take work from both (a graph captured on
+ * the execute stream records both branches).  on = 0 (the default): one stream, the direct queue
+ * first.  The images do not depend on the setting. */
+int sarbp_batch_set_concurrent(sarbp_batch* batch, int on);
 
 /* ---- range compression (sar_io.range_compress, sar_io.py:116-139) --------- */
 
@@ -368,6 +374,15 @@ int sarbp_direct_polar_phase32(const float* data, int pulses, int samples, const
                                const double* weight, const double* phase, const sarbp_polar_grid* grid,
                                double range_start, double data_dr, double k, int wrapped, float* out,
                                void* stream);
+
+/* ---- measurement ----------------------------------------------------------- */
+
+/* FP32 issue-rate microbenchmark on the current device (no counterpart in the reference): eight
+ * independent FMA chains per thread at full occupancy, scalar FFMA (packed = 0) or packed f32x2
+ * FFMA2 (packed = 1), `iters` steps per chain; *tflops = flops (FMA = 2) per second over the
+ * CUDA-event time of one launch after an untimed one.  Synchronises the device.  It is the
+ * measured FP32 denominator of the back-projection kernels' roofline. */
+int sarbp_fp32_peak(int packed, int iters, double* tflops);
 
 #ifdef __cplusplus
 }

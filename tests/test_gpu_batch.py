@@ -149,3 +149,29 @@ def test_autotune_picks_a_measured_candidate(small_batch, tmp_path):
     assert min(timings.values()) == timings[f"{choice[0]},{choice[1]},{choice[2]}"]
     again, _ = tune_direct(sc, cache=tmp_path / "tune.json")
     assert again == choice  # served from the cache
+
+
+def test_concurrent_batch_equals_single_stream_batch(small_batch):
+    """The FFBP chain on the batch's own stream beside the direct queue gives the same images, eagerly
+    and from a captured graph (both branches recorded in one graph)."""
+    from bp_project_gb300.batch import SceneBatch
+    refs = [single(sc) for sc in small_batch]
+    torch.cuda.synchronize()
+    for bps in (2, 4):
+        fresh = [type(sc)(**{**sc.__dict__, "out": None}) for sc in small_batch]
+        batch = SceneBatch(fresh, blocks_per_sm=bps, concurrent=True)
+        batch.execute()
+        torch.cuda.synchronize()
+        for sc, r in zip(fresh, refs):
+            assert torch.equal(sc.out, r), (bps, type(sc).__name__)
+        batch.capture_graph()
+        for o in batch.outputs:
+            o.zero_()
+        for _ in range(2):
+            batch.replay()
+        torch.cuda.synchronize()
+        for sc, r in zip(fresh, refs):
+            assert torch.equal(sc.out, r), (bps, "graph", type(sc).__name__)
+        lat = batch.scene_latencies_ms()
+        assert len(lat) == len(fresh) and np.all(lat > 0)
+        batch.close()
