@@ -373,17 +373,19 @@ def run_autofocus(args, rank):
     print(json.dumps(line), flush=True)
 
 
-def batch_measure(dev, scenes_count, steps, warmup):
-    """64 independent scenes of uneven size (half direct BP, half FFBP) as one CUDA graph of
-    persistent work-queue launches, tile shapes from the autotuner; against the same scenes
-    formed one at a time through the single-scene entry points.  Returns the measurement dict."""
+def batch_measure(dev, scenes_count, steps, warmup, pulse_choices=None, side_choices=(256, 512, 1024, 2048),
+                  tune=True):
+    """Independent scenes of uneven size (half direct BP, half FFBP) as one CUDA graph of
+    persistent work-queue launches, tile shapes from the autotuner (``tune``); against the same
+    scenes formed one at a time through the single-scene entry points.  Returns the measurement
+    dict.  The defaults are the 64-scene workload: pulses U{512..8192}, sides U{256..2048}."""
     import torch
 
     from bp_project_gb300 import autotune, core, scenes
     from bp_project_gb300.batch import DirectScene, FFBPScene, SceneBatch
     from bp_project_gb300.gpu_backend import build_ffbp_plan
     t0 = time.perf_counter()
-    cfgs = scenes.batch_configs(count=scenes_count)
+    cfgs = scenes.batch_configs(count=scenes_count, pulse_choices=pulse_choices, side_choices=side_choices)
     items = []
     for cfg, kind in cfgs:
         sc = scenes.synthesize(cfg, device=str(dev))
@@ -405,7 +407,7 @@ def batch_measure(dev, scenes_count, steps, warmup):
     choices = {}
     for sc in items:
         side = max(getattr(sc, "rows", 0), getattr(sc, "cols", 0))
-        if isinstance(sc, DirectScene) and side not in choices:
+        if tune and isinstance(sc, DirectScene) and side not in choices:
             n = min(1024, sc.data.shape[0])
             rep = DirectScene(**{**sc.__dict__, "data": sc.data[:n].contiguous(), "pos": sc.pos[:n].contiguous(),
                                  "weight": sc.weight[:n].contiguous(), "phase": sc.phase[:n].contiguous(),
@@ -418,10 +420,13 @@ def batch_measure(dev, scenes_count, steps, warmup):
             default_ref[i] = core.backproject_lattice(sc.data, sc.pos, sc.weight, sc.phase, sc.origin, sc.step_row,
                                                       sc.step_col, sc.rows, sc.cols, sc.range_start, sc.data_dr,
                                                       sc.k, mode="split", pulse_split=1)
-    autotune.apply(items, choices)
-    blocks, block_timings = autotune.tune_blocks(items)
+    if tune:
+        autotune.apply(items, choices)
+        (blocks, concurrent), block_timings = autotune.tune_blocks(items)
+    else:
+        (blocks, concurrent), block_timings = (0, False), {}
 
-    batch = SceneBatch(items, blocks_per_sm=blocks)
+    batch = SceneBatch(items, blocks_per_sm=blocks, concurrent=concurrent)
     graph = batch.capture_graph()
     for _ in range(max(warmup, 3) - 1):
         batch.replay()
@@ -476,7 +481,8 @@ def batch_measure(dev, scenes_count, steps, warmup):
         "metric": "batched scenes: Gpixel·pulses/s (direct-equivalent) and scenes/s", "value": px / (batch_ms / 1e3) / 1e9,
         "unit": "Gpixel·pulses/s", "higher_is_better": True, "n_gpus": 1, "steps": steps,
         "warmup": warmup, "ms_per_step": batch_ms, "data": "synthetic", "dtype": "f32 (split precision)",
-        "config": {"workload": f"{len(items)} scenes: pulses U{{512..8192 step 512}}, side U{{256,512,1024,2048}} "
+        "config": {"workload": f"{len(items)} scenes: pulses U{{{','.join(str(int(p)) for p in pulse_choices) if pulse_choices is not None else '512..8192 step 512'}}}, "
+                               f"side U{{{','.join(str(v) for v in side_choices)}}} "
                                "@0.5 m, half direct BP / half FFBP (leaf 16), near slant U(3.5, 8) km, 4-16 "
                                "targets + 256 clutter, 9.6 GHz / 150 MHz",
                    "scenes": len(items), "direct_pixel_pulses": direct_px, "all_pixel_pulses": px,
@@ -484,9 +490,11 @@ def batch_measure(dev, scenes_count, steps, warmup):
                        sum(sc.data.numel() * 8 for sc in items) / 1e9)},
         "scenes_per_s": len(items) / (batch_ms / 1e3),
         "graph": "one CUDA graph per batch: %d launches (memset, 3 FFBP prologues, persistent direct and leaf launches, %d persistent "
-                 "merge levels)" % (batch.launch_count, batch.info["max_height"]),
+                 "merge levels)%s" % (batch.launch_count, batch.info["max_height"],
+                                      "; the FFBP chain on a forked branch beside the direct queue" if concurrent
+                                      else ""),
         "batch_info": batch.info, "autotune": {str(k): list(v) for k, v in choices.items()},
-        "autotune_blocks_per_sm": {"chosen": blocks, "ms": block_timings},
+        "autotune_blocks_per_sm": {"chosen": blocks, "concurrent": concurrent, "ms": block_timings},
         "autotune_s": tune_s, "synthesis_s": synth_s,
         "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / batch_ms,
         "sequential_clocks": seq_clocks.summary(),
@@ -745,6 +753,11 @@ def main():
                 "scene_latency_ms", "graph", "gpu_launches", "clocks", "sequential_clocks",
                 "tuned_vs_default_shape_err_max", "autotune", "autotune_blocks_per_sm", "autotune_s", "synthesis_s")
         extra["batch"] = {"workload": b["config"]["workload"], **{k_: b[k_] for k_ in keep}}
+        # Many small scenes, where one-at-a-time forming leaves the GPU idle between short launches.
+        b = batch_measure(dev, 256, steps=min(args.steps, 5), warmup=args.warmup, pulse_choices=(512, 1024),
+                          side_choices=(256, 512), tune=False)
+        extra["batch_small"] = {"workload": b["config"]["workload"],
+                                **{k_: b[k_] for k_ in keep if k_ not in ("autotune", "autotune_blocks_per_sm")}}
 
     if rank != 0:
         if world > 1:
@@ -759,7 +772,11 @@ def main():
     achieved_gbs = alg_bytes / (kernel_ms / 1e3) / 1e9
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_derived = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    # Measured FP32 issue rate (sarbp_fp32_peak: independent FMA chains at full occupancy), the
+    # better of scalar FFMA and packed FFMA2, taken right after the timed region.
+    fp32_measured = {"ffma": core.fp32_peak_tflops(packed=False), "ffma2": core.fp32_peak_tflops(packed=True)}
+    fp32_peak = max(fp32_measured.values())
     fp32_achieved = units * FP32_FLOPS_PER_PX_PULSE / (kernel_ms / 1e3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -781,10 +798,12 @@ def main():
                      "kernel": "split_lattice_kernel", "note": f"peak of {peak_kind}; algorithmic bytes "
                      f"{alg_bytes / 1e6:.1f} MB per launch; the kernel is FP32/MUFU-issue bound (roofline_fp32)"},
         "roofline_fp32": {"bound": "fp32_issue", "achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                          "frac": fp32_achieved / fp32_peak,
+                          "frac": fp32_achieved / fp32_peak, "peak_kind": "measured",
+                          "peak_measured": fp32_measured, "peak_derived": fp32_derived,
                           "note": f"{FP32_FLOPS_PER_PX_PULSE:.0f} algorithmic FP32 flops + {MUFU_PER_PX_PULSE:.0f} "
-                                  f"MUFU per pixel-pulse; peak = {sm_count} SMs x 128 lanes x 2 x median SM clock "
-                                  f"{sm_mhz:.0f} MHz (no measured FP32 peak available)"},
+                                  f"MUFU per pixel-pulse; peak measured on this GPU in this run (sarbp_fp32_peak, "
+                                  f"independent FMA chains at full occupancy); derived {sm_count} SMs x 128 lanes x "
+                                  f"2 x median SM clock {sm_mhz:.0f} MHz = {fp32_derived:.1f}"},
         "kernel_ms": kernel_ms,
         "clocks": clk,
         "gpu_launches": int(launches),
