@@ -44,13 +44,19 @@ def _stale() -> bool:
     return any(p.stat().st_mtime > built for p in deps)
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> Path:
-    """Compile and link libsarbp.so if any source is newer than the library."""
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, bulk_windows: bool = False) -> Path:
+    """Compile and link libsarbp.so if any source is newer than the library.
+
+    ``bulk_windows`` builds the measured alternative in which the direct kernels' range windows
+    arrive in shared memory by cp.async.bulk copies (SARBP_BULK_WINDOWS); it is 2% slower than the
+    default on the 4096-pulse lattice and is not the default.  Rebuild with force=True to switch."""
     if not force and not _stale():
         return LIBRARY
     BUILD.mkdir(exist_ok=True)
     compiler = nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
+    if bulk_windows:
+        extra += ["-DSARBP_BULK_WINDOWS=1"]
 
     def compile_one(src: Path):
         obj = BUILD / (src.stem + ".o")
@@ -78,4 +84,5 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, ptxas_info="--ptxas" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, ptxas_info="--ptxas" in sys.argv,
+                bulk_windows="--bulk-windows" in sys.argv))

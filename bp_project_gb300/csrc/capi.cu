@@ -132,6 +132,9 @@ namespace {
 
 // Window radius assumed for point tiles: pulses of wider tiles run through the two-float fallback.
 constexpr double kPointRadius = 24.0;
+// Split-mode merge tiles may be up to this factor wider (in radius) than the squarest shape:
+// a warp's pixels then span fewer rows, and its stencil gathers fewer sectors.
+constexpr double kMergeTileSlack = 1.5;
 
 }  // namespace
 
@@ -508,6 +511,7 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         p->max_dim = std::max(p->max_dim, std::max(d.nr, d.nu));
         double radius = 0.0;
         d.tile_lc = split_polar_tile_lc(d, &radius);
+        if (d.left >= 0 && mode == SARBP_SPLIT) d.tile_lc = split_polar_tile_lc_slack(d, kMergeTileSlack, nullptr);
         if (d.left < 0 && mode == SARBP_SPLIT) {
             // Leaves use the origin formulation: precision does not depend on the tile shape, and
             // 32-row tiles keep each pulse's range window short.

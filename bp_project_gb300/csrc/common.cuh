@@ -185,6 +185,8 @@ int split_lattice_auto_split(const sarbp_lattice& lat, int pulses);
 // Tile column exponent (2..5) that makes a polar tile of grid g closest to square in metres,
 // and the largest pixel offset from the tile centre (metres) over the grid for that shape.
 int split_polar_tile_lc(const PolarDesc& g, double* radius);
+// The widest tile shape whose radius is within `slack` (>= 1) of the smallest (FFBP merge tiles).
+int split_polar_tile_lc_slack(const PolarDesc& g, double slack, double* radius);
 int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_split, int chunk, int window_bins,
                        float2* out, long long out_stride, long long split_stride, cudaStream_t s);
 int launch_split_lattice(const PulseInputs& in, const sarbp_lattice& lat, int pulse_split, int chunk,

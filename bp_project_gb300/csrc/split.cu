@@ -54,6 +54,18 @@ constexpr int kWindowBudget = 68 * 1024;
 // usual geometries need 15-25 bins per pulse, so 64-pulse chunks mostly fit; wider windows
 // just fit fewer pulses per chunk (the image does not depend on the chunking).
 constexpr int kLatticeWindowBudget = 49 * 1024;
+#ifndef SARBP_BULK_WINDOWS
+#define SARBP_BULK_WINDOWS 0
+#endif
+// Bulk-copy window staging (SARBP_BULK_WINDOWS = 1): each pulse's raw samples arrive in shared
+// memory by one cp.async.bulk copy (completion on an mbarrier) before the Horner transform,
+// instead of the transform's own global loads.  The raw samples need room beside the windows:
+// per window bin 8 bytes plus five samples of margin per pulse, so the window budgets shrink to
+// keep the same CTAs per SM.
+constexpr int kBulkMargin = 5;
+__host__ __device__ constexpr int raw_bytes_for(int cap, int chunk) {
+    return SARBP_BULK_WINDOWS ? (cap + kBulkMargin * chunk) * 8 + 16 : 0;
+}
 // K rho^2 / R limits (turns) for the FP32 eps term: direct BP targets 1e-5 relative
 // error, FFBP leaves 1e-4.
 constexpr double kDirectEnvelope = 8.0;
@@ -92,6 +104,10 @@ struct TileShared {
     int wsum;                   // window entries of record warp 0's pulses
     float sth[6], stl[6];       // lattice tiles: step_row (0-2) and step_col (3-5) as two-float
     int row_step;               // lattice tiles: rows between a thread's successive pixels
+#if SARBP_BULK_WINDOWS
+    int roff[kMaxChunk];        // bulk staging: first raw sample of each pulse in shared memory
+    long long raw0[kMaxChunk];  // bulk staging: data-array index of that sample
+#endif
 };
 
 // Row/column tables of a polar tile; aliased onto the window region during set-up.
@@ -592,19 +608,8 @@ __device__ __forceinline__ void polar_chunk(const SplitParams& P, const Rec* __r
     static_assert(kPX == 4, "two pixel pairs per thread");
     const float2 ninv = pair(-P.inv_drf), nKf = pair(-P.Kf), mone = pair(-1.0f), mtwo = pair(-2.0f);
     const float2 magic = pair(kMagic), nmagic = pair(-kMagic), twopi = pair(kTwoPiF);
-    float2 dx[2], dy[2], dxh[2], dyh[2], dxl[2], dyl[2], nd2[2], psi[2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const Pix &a = px[2 * h], &b = px[2 * h + 1];
-        dx[h] = make_float2(a.dx, b.dx);
-        dy[h] = make_float2(a.dy, b.dy);
-        dxh[h] = make_float2(a.dxh, b.dxh);
-        dyh[h] = make_float2(a.dyh, b.dyh);
-        dxl[h] = make_float2(a.dxl, b.dxl);
-        dyl[h] = make_float2(a.dyl, b.dyl);
-        nd2[h] = make_float2(-a.d2, -b.d2);
-        psi[h] = make_float2(a.psi, b.psi);
-    }
+    for (int k = 0; k < kPX; ++k) px[k].d2 = -px[k].d2;  // carried as -d2 through the chunk
 #pragma unroll 1
     for (int nl = 0; nl < chn; ++nl) {
         const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c;
@@ -615,8 +620,10 @@ __device__ __forceinline__ void polar_chunk(const SplitParams& P, const Rec* __r
         const float2 Wx = pair(ra.x), Wy = pair(ra.y), Wlx = pair(ra.z), Wly = pair(ra.w), phi = pair(rc.x);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const float2 nL = __ffma2_rn(nux, dx[h], __fmul2_rn(nuy, dy[h]));
-            const float2 nq2 = __ffma2_rn(nL, nL, nd2[h]);
+            const Pix &pa = px[2 * h], &pb = px[2 * h + 1];
+            const float2 dx = make_float2(pa.dx, pb.dx), dy = make_float2(pa.dy, pb.dy);
+            const float2 nL = __ffma2_rn(nux, dx, __fmul2_rn(nuy, dy));
+            const float2 nq2 = __ffma2_rn(nL, nL, make_float2(pa.d2, pb.d2));
             const float2 den = __ffma2_rn(mtwo, nL, twoR);
             const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
             const float2 ne0 = __fmul2_rn(nq2, B);
@@ -624,13 +631,13 @@ __device__ __forceinline__ void polar_chunk(const SplitParams& P, const Rec* __r
             const float2 qp = __ffma2_rn(__fadd2_rn(nL, neps), ninv, fm);
             const float2 tq = __fadd2_rn(qp, magic);
             const float2 sv = __ffma2_rn(__fadd2_rn(tq, nmagic), mone, qp);
-            const float2 tb = __ffma2_rn(Wx, dxh[h], __fmul2_rn(Wy, dyh[h]));  // exact
+            const float2 tb = __ffma2_rn(Wx, make_float2(pa.dxh, pb.dxh), __fmul2_rn(Wy, make_float2(pa.dyh, pb.dyh)));
             float2 sm = __ffma2_rn(nKf, neps, phi);
-            sm = __ffma2_rn(Wx, dxl[h], sm);
-            sm = __ffma2_rn(Wy, dyl[h], sm);
-            sm = __ffma2_rn(Wlx, dx[h], sm);
-            sm = __ffma2_rn(Wly, dy[h], sm);
-            sm = __fadd2_rn(sm, psi[h]);
+            sm = __ffma2_rn(Wx, make_float2(pa.dxl, pb.dxl), sm);
+            sm = __ffma2_rn(Wy, make_float2(pa.dyl, pb.dyl), sm);
+            sm = __ffma2_rn(Wlx, dx, sm);
+            sm = __ffma2_rn(Wly, dy, sm);
+            sm = __fadd2_rn(sm, make_float2(pa.psi, pb.psi));
             // The reduced large term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps <= 1 + envelope / 2
             // turns, so the angle stays within +-40 rad, which the hardware sin/cos reduce themselves.
             const float2 rtb = __fadd2_rn(__fadd2_rn(tb, magic), nmagic);
@@ -654,6 +661,8 @@ __device__ __forceinline__ void polar_chunk(const SplitParams& P, const Rec* __r
             }
         }
     }
+#pragma unroll
+    for (int k = 0; k < kPX; ++k) px[k].d2 = -px[k].d2;
 }
 
 // ---- two-float arithmetic (unevaluated sums hi + lo of two FP32 numbers) ----------------
@@ -922,6 +931,104 @@ __device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* s
     return make_float2(ar, ai);
 }
 
+#if SARBP_BULK_WINDOWS
+__device__ int g_bulk_timeouts;  // bulk-copy waits that ran out (the staged windows are then invalid)
+
+// Raw samples [b - 1, b + cnt + 2) of each fitting pulse's row (clipped to the row) arrive in
+// shared memory by one 1-D cp.async.bulk copy per pulse, issued by warp 0 after lane 0 has set
+// the transaction count on the mbarrier; every thread waits for the phase (a bounded wait that
+// records a timeout), then the Horner transform reads shared memory.  A copy must start and end
+// on 16-byte boundaries of the data array, so the copied range is widened to even elements.
+__device__ __forceinline__ void bulk_stage_windows(const SplitParams& P, TileShared& S, const Rec* rec, float4* win,
+                                                   float2* raw, unsigned long long& mbar, unsigned phase, int c0,
+                                                   int nfit, bool weighted) {
+    const PulseInputs& in = P.in;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&mbar);
+    if (warp == 0) {
+        long long a0[2];
+        int len[2];
+        int mine = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int nl = lane + 32 * h;
+            a0[h] = 0;
+            len[h] = 0;
+            if (nl < nfit) {
+                const long long row0 = (long long)(c0 + nl) * in.samples;
+                const long long b0 = S.base[nl];
+                const int cnt = __float_as_int(rec[nl].c.w) + 1;
+                // [g0, g1) within the row; rows start on even elements (samples is even), so
+                // widening to even bounds stays inside the row.
+                const long long g0 = min(max(b0 - 1, 0ll), (long long)in.samples);
+                const long long g1 = max(min(b0 + cnt + 2, (long long)in.samples), g0);
+                const long long e0 = (row0 + g0) & ~1ll, e1 = (row0 + g1 + 1) & ~1ll;
+                a0[h] = e0;
+                len[h] = (int)max(e1 - e0, 0ll);
+                mine += len[h];
+            }
+        }
+        // Exclusive prefix of the raw lengths (even, so every destination stays 16-byte aligned).
+        int inc = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, inc, 31);
+        int off = inc - mine;
+        if (lane == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(total * 8)
+                         : "memory");
+        }
+        __syncwarp();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the last chunk's reads precede these writes
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int nl = lane + 32 * h;
+            if (nl < nfit) {
+                S.roff[nl] = off;
+                S.raw0[nl] = a0[h];
+                if (len[h] > 0) {
+                    const unsigned dst = (unsigned)__cvta_generic_to_shared(raw + off);
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            dst),
+                        "l"(in.data + a0[h]), "r"(len[h] * 8), "r"(bar)
+                        : "memory");
+                }
+                off += len[h];
+            }
+        }
+    }
+    // Bounded wait for the copies of this chunk's phase.
+    unsigned done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it)
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+    if (!done && threadIdx.x == 0) atomicAdd(&g_bulk_timeouts, 1);
+    __syncthreads();  // roff / raw0 written by warp 0
+    for (int nl = warp; nl < nfit; nl += kThreads / 32) {
+        const int woff = __float_as_int(rec[nl].c.z);
+        const int cnt = __float_as_int(rec[nl].c.w) + 1;
+        const long long b0 = S.base[nl];
+        const float a = weighted ? S.wt[nl] : 1.0f;
+        const float2* r = raw + S.roff[nl] + ((long long)(c0 + nl) * in.samples - S.raw0[nl]);  // row-relative
+        for (int j = lane; j < cnt; j += 32) {
+            const long long g = b0 + j;
+            float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
+            if (g >= 1 && g <= (long long)in.samples - 3)
+                cubic_coefficients(r[g - 1], r[g], r[g + 1], r[g + 2], a, c01, c23);
+            win[2 * (woff + j)] = c01;
+            win[2 * (woff + j) + 1] = c23;
+        }
+    }
+}
+#endif
+
 // Chunk driver shared by the forward and adjoint kernels: per chunk of up to 64
 // pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, two-float,
 // on two SM sub-partitions at once) and pack the pulses' range windows, all warps
@@ -935,6 +1042,17 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
     Rec* rec = reinterpret_cast<Rec*>(smem);
     float4* win = reinterpret_cast<float4*>(smem + window_offset());
     SlowRec* slow = reinterpret_cast<SlowRec*>(win);  // a chunk that stages nothing reuses the window space
+#if SARBP_BULK_WINDOWS
+    float2* raw = reinterpret_cast<float2*>(smem + window_offset() + (size_t)P.cap * 32);
+    __shared__ __align__(8) unsigned long long mbar;
+    unsigned phase = 0;
+    // Bulk copies need 16-byte aligned rows: an even sample count on a 16-byte aligned array.
+    const bool bulk = ((reinterpret_cast<uintptr_t>(in.data) & 15) == 0) && (in.samples % 2 == 0);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((unsigned)__cvta_generic_to_shared(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+#endif
     if (threadIdx.x == 0) {  // the tile centre as two-float for the records (ordered by the loop's barrier)
         split2(S.cx, S.ch[0], S.cl[0]);
         split2(S.cy, S.ch[1], S.cl[1]);
@@ -964,6 +1082,12 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
         __syncthreads();
         const int nfit = S.nfit_w[0] + S.nfit_w[1];
         if (nfit > 0) {
+#if SARBP_BULK_WINDOWS
+            if (bulk) {
+                bulk_stage_windows(P, S, rec, win, raw, mbar, phase, c0, nfit, weighted);
+                phase ^= 1u;
+            } else
+#endif
             for (int nl = warp; nl < nfit; nl += kThreads / 32) {
                 const int off = __float_as_int(rec[nl].c.z);
                 const int cnt = __float_as_int(rec[nl].c.w) + 1;
@@ -1002,6 +1126,11 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
             c0 += nslow;
         }
     }
+#if SARBP_BULK_WINDOWS
+    __syncthreads();  // every wait on the barrier is over: it can be invalidated (and initialised again)
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"((unsigned)__cvta_generic_to_shared(&mbar)) : "memory");
+#endif
 }
 
 template <bool HAS_Z, bool DEMOD>
@@ -2277,7 +2406,7 @@ size_t merge_smem() { return sizeof(TabF); }
 size_t dynamic_smem(int cap, bool polar) {
     size_t win = (size_t)cap * 32;
     if (polar && win < sizeof(PolarTables)) win = sizeof(PolarTables);
-    return window_offset() + win;
+    return window_offset() + win + raw_bytes_for(cap, kMaxChunk);
 }
 
 template <class K>
@@ -2323,7 +2452,10 @@ int tiles_of(int nr, int nu, int lc) {
 // `window_bins` bins each (the kernel packs the actual, usually smaller, windows).
 int capacity_for(int chunk, int window_bins, int budget_bytes = kWindowBudget) {
     long long cap = (long long)chunk * window_bins;
-    const long long budget = budget_bytes / 32;
+    // With bulk staging a window bin also needs 8 bytes of raw samples (plus a fixed margin).
+    // (2 KB more are left for the bulk path's larger static shared memory.)
+    const long long budget =
+        SARBP_BULK_WINDOWS ? (budget_bytes - raw_bytes_for(0, kMaxChunk) - 2048) / 40 : budget_bytes / 32;
     return (int)(cap > budget ? budget : cap);
 }
 
@@ -2345,7 +2477,9 @@ int split_chunk_for(int window_bins, int requested, bool leaf) {
     return ch < 1 ? 1 : ch;
 }
 
-int split_polar_tile_lc(const PolarDesc& g, double* radius) {
+int split_polar_tile_lc(const PolarDesc& g, double* radius) { return split_polar_tile_lc_slack(g, 1.0, radius); }
+
+int split_polar_tile_lc_slack(const PolarDesc& g, double slack, double* radius) {
     // Ground displacement per range row <= dr * r / g; per angle column <= du * g / sqrt(1 - u^2).
     const double rmin = g.r0 + g.win_r0 * g.dr, rmax = g.r0 + (g.win_r0 + g.win_nr - 1) * g.dr;
     const double gmin = sqrt(fmax(1e-6, rmin * rmin - g.oz * g.oz));
@@ -2354,17 +2488,25 @@ int split_polar_tile_lc(const PolarDesc& g, double* radius) {
     const double cmin = sqrt(fmax(1e-6, 1.0 - fmax(ua, ub) * fmax(ua, ub)));
     const double per_row = fabs(g.dr) * fmax(rmin, rmax) / gmin;
     const double per_col = fabs(g.du) * gmax / cmin;
+    double rads[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     int best = 5;
     double best_r = 1e300;
     for (int lc = 2; lc <= 5; ++lc) {
         const double er = (kSplitTilePixels >> lc) * per_row, eu = (1 << lc) * per_col;
-        const double rad = 0.5 * sqrt(er * er + eu * eu) * 1.05;
-        if (rad < best_r) {
-            best_r = rad;
+        rads[lc] = 0.5 * sqrt(er * er + eu * eu) * 1.05;
+        if (rads[lc] < best_r) {
+            best_r = rads[lc];
             best = lc;
         }
     }
-    if (radius) *radius = best_r;
+    // The widest shape within `slack` of the smallest radius (wider tiles keep a warp's pixels in
+    // fewer rows).
+    for (int lc = 5; lc > best; --lc)
+        if (rads[lc] <= slack * best_r) {
+            best = lc;
+            break;
+        }
+    if (radius) *radius = rads[best];
     return best;
 }
 
@@ -2386,7 +2528,7 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
 // largest window budget, so that it depends on the lattice only and the workspace query and the
 // launch agree (fewer pulses only lower it).
 int split_lattice_auto_split(const sarbp_lattice& lat, int pulses) {
-    const size_t smem = dynamic_smem(kLatticeWindowBudget / 32, false);
+    const size_t smem = dynamic_smem(capacity_for(kMaxChunk, 1 << 20, kLatticeWindowBudget), false);
     if (prepare(split_lattice_kernel, smem) != SARBP_OK) return 1;
     return best_pulse_split(split_lattice_kernel, smem, tiles_of(lat.rows, lat.cols, 5), pulses);
 }
@@ -2704,7 +2846,8 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     b.lc = d.lc;
     b.prec_offset = d.prec_offset;
     memcpy(dst, &b, sizeof(b));
-    return (d.kind == 0 ? window_offset() : (size_t)kMaxLeafChunk * sizeof(LeafRec)) + (size_t)b.P.cap * 32;
+    return (d.kind == 0 ? window_offset() + raw_bytes_for(b.P.cap, kMaxChunk) : (size_t)kMaxLeafChunk * sizeof(LeafRec)) +
+           (size_t)b.P.cap * 32;
 }
 
 int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_sm, int* leaf_per_sm,

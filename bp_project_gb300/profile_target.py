@@ -7,7 +7,9 @@ its kernels:
     python -m bp_project_gb300.profile_target --workload ffbp   --config c1 --reps 2
 
 Workloads: ``direct`` (split-precision direct BP on the scene's ground
-lattice), ``ffbp`` (level-batched FFBP + split evaluation onto the lattice),
+lattice), ``polar`` (split-precision direct BP onto a 1024 x 4096 window of the
+scene's FFBP root polar grid, the ``CudaBaseline.run_direct`` surface),
+``ffbp`` (level-batched FFBP + split evaluation onto the lattice),
 ``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice),
 ``adjoint`` (forward + adjoint of lattice BP, the entropy autofocus step),
 ``range`` (range compression of the scene's data treated as raw echoes),
@@ -87,7 +89,7 @@ def _all_kernels(scene, data, pos, wt, ph, dev):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=("direct", "ffbp", "plain", "adjoint", "range", "batch", "all"),
+    ap.add_argument("--workload", choices=("direct", "polar", "ffbp", "plain", "adjoint", "range", "batch", "all"),
                     default="direct")
     ap.add_argument("--config", default="c1")
     ap.add_argument("--pulses", type=int, default=None, help="scale the scene to this many pulses")
@@ -119,6 +121,19 @@ def main(argv=None):
             core.backproject_lattice(data, pos, wt, ph, lat.origin, lat.step_row, lat.step_col, rows, lat.cols,
                                      scene.range_start, scene.data_dr, scene.k, mode=mode, out=out)
         units = rows * lat.cols * cfg.pulses
+    elif args.workload == "polar":
+        plan = build_ffbp_plan(scene.position, cfg.fc, scene.extent, side=1, leaf_size=cfg.leaf_size,
+                               range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+        g = plan.grid()
+        nr, nu = min(1024, g.nr), min(4096, g.nu)
+        r_off, u_off = (g.nr - nr) // 2, (g.nu - nu) // 2
+        sub = core.Grid(g.origin, g.r0 + r_off * g.dr, g.dr, nr, g.u0 + u_off * g.du, g.du, nu, g.side)
+        out = torch.empty((nr, nu), dtype=torch.complex64, device=dev)
+
+        def run():
+            core.direct_polar(data, pos, wt, ph, sub, scene.range_start, scene.data_dr, scene.k, mode=args.mode,
+                              out=out)
+        units = nr * nu * cfg.pulses
     elif args.workload == "all":
         run = _all_kernels(scene, data, pos, wt, ph, dev)
         units = lat.rows * lat.cols * cfg.pulses
