@@ -173,6 +173,11 @@ const char* sarbp_status_string(int status) {
 }
 
 const char* sarbp_last_error(void) { return g_last_error.c_str(); }
+
+int sarbp_wait_timeouts(int* count) {
+    if (!count) return fail(SARBP_ERR_TYPE, "count must not be NULL");
+    return split_wait_timeouts(count);
+}
 uint64_t sarbp_launch_count(void) { return g_launches.load(); }
 
 // ---- direct BP ---------------------------------------------------------------------------

@@ -182,6 +182,8 @@ double lattice_radius(const sarbp_lattice& lat, int lc);
 // Pulses per shared-memory chunk that fit `window_bins` within the shared-memory budget.
 int split_chunk_for(int window_bins, int requested, bool leaf = false);
 int split_lattice_auto_split(const sarbp_lattice& lat, int pulses);
+// Bounded waits in the kernels that ran out since the library was loaded (synchronises).
+int split_wait_timeouts(int* count);
 // Tile column exponent (2..5) that makes a polar tile of grid g closest to square in metres,
 // and the largest pixel offset from the tile centre (metres) over the grid for that shape.
 int split_polar_tile_lc(const PolarDesc& g, double* radius);

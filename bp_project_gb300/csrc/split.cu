@@ -939,7 +939,21 @@ __device__ int g_bulk_timeouts;  // bulk-copy waits that ran out (the staged win
 // the transaction count on the mbarrier; every thread waits for the phase (a bounded wait that
 // records a timeout), then the Horner transform reads shared memory.  A copy must start and end
 // on 16-byte boundaries of the data array, so the copied range is widened to even elements.
-__device__ __forceinline__ void bulk_stage_windows(const SplitParams& P, TileShared& S, const Rec* rec, float4* win,
+// Bounded wait for the phase `phase` of the mbarrier at shared address bar; true once it completed.
+__device__ __forceinline__ bool bulk_wait(unsigned bar, unsigned phase) {
+    unsigned done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it)
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+    return done != 0;
+}
+
+// Returns false (the same in every thread) if the copies did not arrive within the bounded wait;
+// the caller then stops staging and waits once more before leaving.
+__device__ __forceinline__ bool bulk_stage_windows(const SplitParams& P, TileShared& S, const Rec* rec, float4* win,
                                                    float2* raw, unsigned long long& mbar, unsigned phase, int c0,
                                                    int nfit, bool weighted) {
     const PulseInputs& in = P.in;
@@ -1002,15 +1016,11 @@ __device__ __forceinline__ void bulk_stage_windows(const SplitParams& P, TileSha
         }
     }
     // Bounded wait for the copies of this chunk's phase.
-    unsigned done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it)
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(bar), "r"(phase)
-            : "memory");
-    if (!done && threadIdx.x == 0) atomicAdd(&g_bulk_timeouts, 1);
-    __syncthreads();  // roff / raw0 written by warp 0
+    const bool done = __syncthreads_and(bulk_wait(bar, phase)) != 0;  // also orders roff / raw0 of warp 0
+    if (!done) {
+        if (threadIdx.x == 0) atomicAdd(&g_bulk_timeouts, 1);
+        return false;
+    }
     for (int nl = warp; nl < nfit; nl += kThreads / 32) {
         const int woff = __float_as_int(rec[nl].c.z);
         const int cnt = __float_as_int(rec[nl].c.w) + 1;
@@ -1026,6 +1036,7 @@ __device__ __forceinline__ void bulk_stage_windows(const SplitParams& P, TileSha
             win[2 * (woff + j) + 1] = c23;
         }
     }
+    return true;
 }
 #endif
 
@@ -1084,7 +1095,12 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
         if (nfit > 0) {
 #if SARBP_BULK_WINDOWS
             if (bulk) {
-                bulk_stage_windows(P, S, rec, win, raw, mbar, phase, c0, nfit, weighted);
+                if (!bulk_stage_windows(P, S, rec, win, raw, mbar, phase, c0, nfit, weighted)) {
+                    // The copies did not arrive: the tile's image is invalid (g_bulk_timeouts counts it).
+                    // Wait once more, bounded, for the copies still in flight, then leave.
+                    bulk_wait((unsigned)__cvta_generic_to_shared(&mbar), phase);
+                    break;
+                }
                 phase ^= 1u;
             } else
 #endif
@@ -2527,6 +2543,16 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
 // The pulse split of a direct lattice launch that asks for the automatic one: sized for the
 // largest window budget, so that it depends on the lattice only and the workspace query and the
 // launch agree (fewer pulses only lower it).
+int split_wait_timeouts(int* count) {
+#if SARBP_BULK_WINDOWS
+    const cudaError_t e = cudaMemcpyFromSymbol(count, g_bulk_timeouts, sizeof(int));
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "wait timeouts: %s", cudaGetErrorString(e));
+#else
+    *count = 0;
+#endif
+    return SARBP_OK;
+}
+
 int split_lattice_auto_split(const sarbp_lattice& lat, int pulses) {
     const size_t smem = dynamic_smem(capacity_for(kMaxChunk, 1 << 20, kLatticeWindowBudget), false);
     if (prepare(split_lattice_kernel, smem) != SARBP_OK) return 1;

@@ -384,6 +384,12 @@ int sarbp_direct_polar_phase32(const float* data, int pulses, int samples, const
  * measured FP32 denominator of the back-projection kernels' roofline. */
 int sarbp_fp32_peak(int packed, int iters, double* tflops);
 
+/* Number of bounded waits in the library's kernels that ran out since it was loaded (no
+ * counterpart in the reference); synchronises the device.  The only waiting kernels are those of
+ * the bulk-copy window staging build (SARBP_BULK_WINDOWS): a tile whose range windows did not
+ * arrive in time stops early, so its image is invalid; the default build never waits and reports 0. */
+int sarbp_wait_timeouts(int* count);
+
 #ifdef __cplusplus
 }
 #endif
