@@ -128,6 +128,7 @@ SIGNATURES = {
     "sarbp_direct_polar_phase32": ([_P, _I, _I, _P, _P, _P, ctypes.POINTER(PolarGrid), _D, _D, _D, _I, _P, _P], _I),
     "sarbp_fp32_peak": ([_I, _I, ctypes.POINTER(_D)], _I),
     "sarbp_wait_timeouts": ([ctypes.POINTER(_I)], _I),
+    "sarbp_ffbp_set_node_image": ([_P, _I, _P, _P], _I),
 }
 
 _lock = threading.Lock()

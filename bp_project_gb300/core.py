@@ -322,6 +322,14 @@ class FFBPProgram:
                                                 stream_handle()), "ffbp_execute")
         return out
 
+    def set_node_image(self, node: int, image):
+        """Supply the image (complex64 [nr, nu]) of external node ``node`` (a leaf whose pulse range is
+        [-1, -1)); the copy is enqueued on the current stream, so ``image`` must stay alive until the
+        stream has run it (the next execute on the same stream is ordered after it)."""
+        _require(image, "image", torch.complex64)
+        nat.check(nat.load().sarbp_ffbp_set_node_image(self._handle, int(node), _ptr(image), stream_handle()),
+                  "ffbp_set_node_image")
+
     def close(self):
         if getattr(self, "_handle", None) is not None and self._handle.value:
             nat.load().sarbp_ffbp_plan_destroy(self._handle)

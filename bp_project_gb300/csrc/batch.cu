@@ -148,6 +148,11 @@ int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks
                 delete b;
                 return fail(st, "scene %d: %s", i, sarbp_last_error());
             }
+            if (p->n_external) {
+                sarbp_ffbp_plan_destroy(p);
+                delete b;
+                return fail(SARBP_ERR_PLAN, "scene %d: batched FFBP plans cannot have external nodes", i);
+            }
             for (int n = 0; n < p->n_nodes; ++n)
                 if (p->nodes[n].left < 0 && p->nodes[n].b > s.pulses) {
                     sarbp_ffbp_plan_destroy(p);

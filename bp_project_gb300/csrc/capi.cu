@@ -475,10 +475,18 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
             delete p;
             return fail(SARBP_ERR_PLAN, "node %d: children must follow their parent in pre-order", i);
         }
-        if (leaf && (n.a < 0 || n.b <= n.a)) {
+        // A leaf with the pulse range [-1, -1) is external: its image comes from the caller
+        // (sarbp_ffbp_set_node_image), e.g. a subtree formed on another GPU.
+        const bool external = leaf && n.a == -1 && n.b == -1;
+        if (external && i == 0) {
+            delete p;
+            return fail(SARBP_ERR_PLAN, "the root cannot be an external node");
+        }
+        if (leaf && !external && (n.a < 0 || n.b <= n.a)) {
             delete p;
             return fail(SARBP_ERR_PLAN, "leaf %d: invalid pulse range [%d, %d)", i, n.a, n.b);
         }
+        p->n_external += external ? 1 : 0;
         PolarDesc d = desc_of(g);
         d.a = n.a;
         d.b = n.b;
@@ -517,14 +525,15 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         double radius = 0.0;
         d.tile_lc = split_polar_tile_lc(d, &radius);
         if (d.left >= 0 && mode == SARBP_SPLIT) d.tile_lc = split_polar_tile_lc_slack(d, kMergeTileSlack, nullptr);
-        if (d.left < 0 && mode == SARBP_SPLIT) {
+        const bool external = d.left < 0 && d.a < 0;
+        if (d.left < 0 && mode == SARBP_SPLIT && !external) {
             // Leaves use the origin formulation: precision does not depend on the tile shape, and
             // 32-row tiles keep each pulse's range window short.
             d.tile_lc = 5;
             p->leaves.push_back(i);
             p->max_pulse = std::max(p->max_pulse, d.b);
         }
-        if (d.left < 0) {
+        if (d.left < 0 && !external) {
             leaf_radius = std::max(leaf_radius, radius);
             leaf_pulses = std::max(leaf_pulses, d.b - d.a);
         }
@@ -538,6 +547,7 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         for (int i = 0; i < n_nodes; ++i) {
             if (p->height[i] != h) continue;
             const PolarDesc& d = p->nodes[i];
+            if (d.left < 0 && d.a < 0) continue;  // external: no work, its image is supplied
             if (mode == SARBP_SPLIT) {
                 const int cols_t = 1 << d.tile_lc, rows_t = kSplitTilePixels >> d.tile_lc;
                 for (int r = 0; r < d.win_nr; r += rows_t)
@@ -604,6 +614,21 @@ int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_byt
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "FFBP bind: %s", cudaGetErrorString(e));
     plan->bound = workspace;
     plan->bound_bytes = workspace_bytes;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float* image, void* stream) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (!plan->bound) return fail(SARBP_ERR_PLAN, "sarbp_ffbp_bind must succeed before set_node_image");
+    if (!image) return fail(SARBP_ERR_TYPE, "image must not be NULL");
+    if (node <= 0 || node >= plan->n_nodes) return fail(SARBP_ERR_VALUE, "node %d is not a non-root node", node);
+    const PolarDesc& d = plan->nodes[node];
+    if (!(d.left < 0 && d.a < 0)) return fail(SARBP_ERR_PLAN, "node %d is not an external node", node);
+    if ((uintptr_t)image & 7) return fail(SARBP_ERR_TYPE, "image must be 8-byte aligned");
+    float2* arena = reinterpret_cast<float2*>(reinterpret_cast<char*>(plan->bound) + plan->arena_offset);
+    const cudaError_t e = cudaMemcpyAsync(arena + d.out_offset, image, (size_t)d.nr * d.nu * sizeof(float2),
+                                          cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "set_node_image: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
 

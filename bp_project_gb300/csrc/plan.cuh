@@ -29,4 +29,5 @@ struct sarbp_ffbp_plan {
     void* bound = nullptr;
     size_t bound_bytes = 0;
     int launches = 0;
+    int n_external = 0;           // leaves whose images the caller supplies (pulse range [-1, -1))
 };

@@ -1,4 +1,4 @@
-"""Direct BP over several GPUs, one process per GPU: pixel bands or pulse ranges.
+"""BP over several GPUs, one process per GPU: direct BP by pixel bands or pulse ranges, FFBP by subtrees.
 
 Direct back-projection shards two ways without changing a single bit of the
 image that one GPU forms:
@@ -170,3 +170,139 @@ def direct_polar_pulses(data, pos, weight, phase, grid, range_start, data_dr, k,
     pulses sharded over ranks; returns on ``dst`` the one-GPU image of ``pulse_split = world``."""
     part = polar_pulse_part(data, pos, weight, phase, grid, range_start, data_dr, k, rank=rank, world=world)
     return reduce_in_rank_order(part, rank, world, dst=dst, group=group)
+
+
+# ---- FFBP: subtrees per rank, the top levels on one rank -------------------------------------
+#
+# FFBP's tree is independent below depth d: with 2^d >= world subtrees rooted at depth d, every
+# rank forms its subtrees as ordinary plans (their roots' full images), sends the roots to one rank,
+# and that rank forms the top of the tree as a plan whose leaves are the subtree roots, marked
+# external (pulse range [-1, -1)) and supplied with sarbp_ffbp_set_node_image.  The top merges run
+# the same kernels on the same tiles as the one-GPU plan, so the image is the same bit for bit.
+# Each rank only needs the pulses of its subtrees.
+
+
+class TreeNode:
+    """The NodePlan fields a plan needs (children as objects), for re-rooted and re-leafed trees."""
+
+    __slots__ = ("origin", "r0", "dr", "nr", "u0", "du", "nu", "side", "a", "b", "left", "right")
+
+    def __init__(self, n, a=None, b=None, left=None, right=None):
+        self.origin = tuple(float(v) for v in n.origin)
+        self.r0, self.dr, self.u0, self.du = float(n.r0), float(n.dr), float(n.u0), float(n.du)
+        self.nr, self.nu, self.side = int(n.nr), int(n.nu), int(n.side)
+        self.a = int(n.a) if a is None else a
+        self.b = int(n.b) if b is None else b
+        self.left, self.right = left, right
+
+
+def _children(n):
+    left, right = getattr(n, "left", None), getattr(n, "right", None)
+    return [] if left is None else [left, right]
+
+
+def ffbp_cut(root, parts: int):
+    """Cut the tree under ``root`` (a NodePlan-like object, children as objects) for ``parts`` ranks.
+
+    Returns (subtrees, top, external): ``subtrees`` lists the pre-order node lists of the 2^d subtrees
+    rooted at depth d = ceil(log2 parts) (a leaf shallower than d is its own subtree), in pre-order;
+    ``top`` is the pre-order node list of the tree above them with each subtree root as an external
+    leaf; ``external[s]`` is subtree s's root index in ``top``."""
+    if parts < 1:
+        raise ValueError("parts must be >= 1")
+    depth = max(0, (parts - 1).bit_length())
+    subtrees, top, external = [], [], []
+
+    def preorder(n, out):
+        out.append(n)
+        for c in _children(n):
+            preorder(c, out)
+
+    def copy_tree(n):
+        kids = _children(n)
+        return TreeNode(n, left=copy_tree(kids[0]) if kids else None, right=copy_tree(kids[1]) if kids else None)
+
+    def walk(n, d):
+        if d == depth or not _children(n):
+            nodes = []
+            preorder(copy_tree(n), nodes)
+            subtrees.append(nodes)
+            ext = TreeNode(n, a=-1, b=-1)
+            external.append(ext)
+            return ext
+        t = TreeNode(n)
+        kids = _children(n)
+        t.left, t.right = walk(kids[0], d + 1), walk(kids[1], d + 1)
+        return t
+
+    top_root = walk(root, 0)
+    preorder(top_root, top)
+    index = {id(n): i for i, n in enumerate(top)}
+    return subtrees, top, [index[id(e)] for e in external]
+
+
+def subtree_ranges(n_subtrees: int, parts: int) -> list[tuple[int, int]]:
+    """Contiguous blocks of subtrees per rank: rank r forms subtrees [n r / W, n (r + 1) / W)."""
+    return [(n_subtrees * r // parts, n_subtrees * (r + 1) // parts) for r in range(parts)]
+
+
+def send_images(images, owner_of, rank: int, world: int, dst: int = 0, group=None):
+    """Move every subtree-root image to rank ``dst`` with point-to-point copies.  ``images`` maps
+    subtree index -> complex64 tensor: on its owner the formed image, on ``dst`` a preallocated
+    receive buffer of the right shape.  Returns the complete {subtree: image} on ``dst``, {} elsewhere."""
+    dist = _dist()
+    out = {}
+    for s_, owner in enumerate(owner_of):
+        if owner == dst:
+            if rank == dst:
+                out[s_] = images[s_]
+            continue
+        if rank == owner:
+            dist.send(torch.view_as_real(images[s_].contiguous()), dst=dst, group=group)
+        elif rank == dst:
+            dist.recv(torch.view_as_real(images[s_]), src=owner, group=group)
+            out[s_] = images[s_]
+    return out
+
+
+def ffbp_subtree_images(data, pos, weight, phase, subtrees, subtree_ids, range_start, data_dr, k):
+    """Form the root images (complex64, full grid) of the given subtrees, each as its own plan."""
+    out = {}
+    for s_ in subtree_ids:
+        nodes_s = subtrees[s_]
+        root = nodes_s[0]
+        prog = core.FFBPProgram(nodes_s, (0, root.nr), (0, root.nu), mode="split", device=data.device)
+        out[s_] = prog.execute(data, pos, weight, phase, range_start, data_dr, k).clone()
+        prog.close()  # host-only; the workspace returns to torch's stream-ordered cache
+    return out
+
+
+def ffbp_top(data, pos, weight, phase, top, external, images, crop_r, crop_u, range_start, data_dr, k):
+    """Form the top of the tree from the subtree roots' images: the cropped root image."""
+    prog = core.FFBPProgram(top, crop_r, crop_u, mode="split", device=data.device)
+    for s_, idx in enumerate(external):
+        prog.set_node_image(idx, images[s_])
+    out = prog.execute(data, pos, weight, phase, range_start, data_dr, k).clone()
+    prog.close()
+    return out
+
+
+def ffbp(data, pos, weight, phase, plan, range_start, data_dr, k, *, rank: int, world: int, group=None, dst: int = 0):
+    """Split-precision FFBP of ``plan`` (gpu_backend.build_ffbp_plan) over ``world`` ranks: subtrees per
+    rank, the top levels on rank ``dst``.  Returns the cropped root image on ``dst`` (None elsewhere),
+    equal to core.FFBPProgram's on one GPU."""
+    subtrees, top, external = ffbp_cut(plan.nodes()[0], world)
+    owner_of = [r for r, (b, e) in enumerate(subtree_ranges(len(subtrees), world)) for _ in range(e - b)]
+    mine = [s_ for s_, r in enumerate(owner_of) if r == rank]
+    images = ffbp_subtree_images(data, pos, weight, phase, subtrees, mine, range_start, data_dr, k)
+    if world > 1:
+        if rank == dst:
+            for s_, r in enumerate(owner_of):
+                if r != dst:
+                    root = subtrees[s_][0]
+                    images[s_] = torch.empty((root.nr, root.nu), dtype=torch.complex64, device=data.device)
+        images = send_images(images, owner_of, rank, world, dst=dst, group=group)
+    if rank != dst:
+        return None
+    return ffbp_top(data, pos, weight, phase, top, external, images, plan.crop_r, plan.crop_u, range_start, data_dr,
+                    k)

@@ -324,13 +324,20 @@ int sarbp_crop(const float* in, int src_nu, int r_begin, int u_begin, int nr, in
  * (fast_bp/resident_backend.py:24-319, batched_resident_backend.py:23-157):
  * one launch for all leaves, one per tree height, the root crop fused into the
  * last merge.  create/destroy are host-only; bind uploads the tables into the
- * caller's workspace (synchronous w.r.t. stream); execute only launches. */
+ * caller's workspace (synchronous w.r.t. stream); execute only launches.  A
+ * leaf whose pulse range is [-1, -1) is an external node: the plan does no work
+ * for it and merges the image the caller supplies with sarbp_ffbp_set_node_image. */
 int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r0, int crop_u0,
                            int crop_nr, int crop_nu, int mode, sarbp_ffbp_plan** plan);
 void sarbp_ffbp_plan_destroy(sarbp_ffbp_plan* plan);
 size_t sarbp_ffbp_workspace_bytes(const sarbp_ffbp_plan* plan);
 int sarbp_ffbp_launch_count(const sarbp_ffbp_plan* plan);
 int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_bytes, void* stream);
+/* Supplies the image (complex64 [nr, nu], device, row-major) of an external node: a leaf of the
+ * plan whose pulse range is [-1, -1), formed elsewhere, e.g. a subtree root imaged on another GPU
+ * (bp_project_gb300.shard).  The plan must be bound; the copy is enqueued on `stream` and the plan
+ * never writes the node.  No counterpart in the reference (its trees are formed in one process). */
+int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float* image, void* stream);
 int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulses, int samples,
                        const double* pos, const double* weight, const double* phase, double range_start,
                        double data_dr, double k, float* out, void* stream);

@@ -80,3 +80,25 @@ def test_polar_pulse_ranges_reproduce_the_one_gpu_pulse_split(golden):
     torch.cuda.synchronize()
     assert torch.equal(acc, want)
     assert rel_err(g["case1_direct"], acc.cpu().numpy()) <= 1e-5
+
+
+@pytest.mark.parametrize("world", [2, 3, 4])
+def test_ffbp_subtrees_reproduce_the_one_gpu_image(scene, world):
+    """FFBP over ranks: each rank's subtrees as their own plans, then the top of the tree from the
+    subtree roots' images (external nodes); the image equals the one-GPU plan's bit for bit."""
+    from bp_project_gb300 import core, shard
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    sc, dev, geo = scene
+    cfg = sc.config
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split")
+    want = prog.execute(*dev, sc.range_start, sc.data_dr, sc.k).clone()
+    prog.close()
+    subtrees, top, external = shard.ffbp_cut(plan.nodes()[0], world)
+    images = {}
+    for r, (b, e) in enumerate(shard.subtree_ranges(len(subtrees), world)):  # rank by rank
+        images.update(shard.ffbp_subtree_images(*dev, subtrees, range(b, e), sc.range_start, sc.data_dr, sc.k))
+    got = shard.ffbp_top(*dev, top, external, images, plan.crop_r, plan.crop_u, sc.range_start, sc.data_dr, sc.k)
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
