@@ -112,6 +112,7 @@ def main(argv=None):
     lat = scene.lattice
     torch.cuda.synchronize()
     times = []
+    image_shape = [lat.rows, lat.cols]
     if args.workload in ("direct", "plain"):
         rows = lat.rows if args.workload == "direct" else 64
         out = torch.empty((rows, lat.cols), dtype=torch.complex64, device=dev)
@@ -134,6 +135,7 @@ def main(argv=None):
             core.direct_polar(data, pos, wt, ph, sub, scene.range_start, scene.data_dr, scene.k, mode=args.mode,
                               out=out)
         units = nr * nu * cfg.pulses
+        image_shape = [nr, nu]
     elif args.workload == "all":
         run = _all_kernels(scene, data, pos, wt, ph, dev)
         units = lat.rows * lat.cols * cfg.pulses
@@ -209,7 +211,7 @@ def main(argv=None):
             torch.cuda.nvtx.range_pop()
         torch.cuda.profiler.stop()
     print(json.dumps({"workload": args.workload, "config": cfg.name, "pulses": cfg.pulses,
-                      "image": [lat.rows, lat.cols], "mode": args.mode, "ms": times,
+                      "image": image_shape, "mode": args.mode, "ms": times,
                       "gpix_pulse_per_s": [units / (t / 1e3) / 1e9 for t in times]}), flush=True)
 
 

@@ -358,6 +358,33 @@ def test_c1_ffbp_vs_reference_ffbp(lib):
     assert err <= 1e-4
 
 
+def test_c2_geometry_ffbp_vs_reference_ffbp(lib):
+    """The 30 km precision-stress geometry (10 GHz, 300 MHz, 150 m/s, 1.5 kHz) at 2048 pulses onto a 512^2
+    image at 0.25 m: split FFBP (16-pulse leaves, merge tiles up to 1.5x the squarest radius) within 1e-4
+    of the reference FFBP (oracle restatement of ffbp.form_ffbp on the same plan)."""
+    from bp_project_gb300 import core
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    from oracle import reference as ora
+    sc = _scene("c2", pulses=2048, samples=4096, image_side=512)
+    cfg = sc.config
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split")
+    img = prog.execute(_dev(sc.data, torch.complex64), _dev(sc.position, torch.float64),
+                       _dev(sc.weight, torch.float64), _dev(sc.phase, torch.float64), sc.range_start, sc.data_dr,
+                       sc.k).cpu().numpy()
+    prog.close()
+    ref, counts = ora.form_ffbp(sc.data, sc.position, sc.range_start, sc.data_dr, cfg.fc, sc.extent, side=1,
+                                leaf_size=cfg.leaf_size, range_spacing=cfg.range_spacing,
+                                angular_oversample=cfg.angular_oversample, weight=sc.weight, phase=sc.phase)
+    assert counts["leaves"] == 128
+    err = rel_err(ref.image, img)
+    print(f"c2-geometry split FFBP vs reference FFBP: {err:.3e}")
+    assert err <= 1e-4
+    peak_ref = np.unravel_index(np.abs(ref.image).argmax(), ref.image.shape)
+    assert np.unravel_index(np.abs(img).argmax(), img.shape) == peak_ref
+
+
 def test_linearity_and_pulse_split(lib):
     """BP is linear in the data; splitting the aperture over CTAs changes only FP32 rounding."""
     from bp_project_gb300 import scenes
