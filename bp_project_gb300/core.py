@@ -288,7 +288,8 @@ def node_array(nodes):
 
 
 class FFBPProgram:
-    """Level-batched FFBP over a node tree (one launch for the leaves, one per height).
+    """Level-batched FFBP over a node tree (one launch for the leaves, one per height; in split mode
+    ``merge_queue=True`` runs the merges as one dependency-counting queue launch instead).
 
     ``nodes`` is a pre-order sequence of objects with the NodePlan fields
     (origin, r0, dr, nr, u0, du, nu, side, a, b, left/right children).  The
@@ -296,7 +297,7 @@ class FFBPProgram:
     directly.  The workspace (node images + device tables) is allocated once.
     """
 
-    def __init__(self, nodes, crop_r, crop_u, mode=DEFAULT_MODE, device="cuda"):
+    def __init__(self, nodes, crop_r, crop_u, mode=DEFAULT_MODE, device="cuda", merge_queue=False):
         self.mode = mode
         arr = node_array(nodes)
         self.crop = (int(crop_r[0]), int(crop_u[0]), int(crop_r[1] - crop_r[0]), int(crop_u[1] - crop_u[0]))
@@ -305,6 +306,9 @@ class FFBPProgram:
         nat.check(lib.sarbp_ffbp_plan_create(arr, len(nodes), *self.crop, nat.mode_id(mode), ctypes.byref(handle)),
                   "ffbp_plan_create")
         self._handle = handle
+        if merge_queue:
+            # all merge levels as one dependency-counting launch instead of one launch per tree height
+            nat.check(lib.sarbp_ffbp_set_merge_queue(handle, 1), "ffbp_set_merge_queue")
         self.workspace_bytes = int(lib.sarbp_ffbp_workspace_bytes(handle))
         self.launch_count = int(lib.sarbp_ffbp_launch_count(handle))
         self.workspace = torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8, device=device)

@@ -573,10 +573,30 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         p->prec_bytes = align_up(split_ffbp_pulse_record_bytes() * (size_t)p->max_pulse);
         p->crec_bytes = align_up(split_ffbp_child_record_bytes() * 2 * (size_t)p->merge_items);
     }
+    if (mode == SARBP_SPLIT) {
+        // Merge queue: per node its merge tiles, its merge children (leaves and external nodes are
+        // complete before the queue starts) and its parent.
+        p->q_remaining.assign(n_nodes, 0);
+        p->q_pending.assign(n_nodes, 0);
+        p->q_parent.assign(n_nodes, -1);
+        for (int i = 0; i < n_nodes; ++i) {
+            const PolarDesc& d = p->nodes[i];
+            if (d.left < 0) continue;
+            for (int c : {d.left, d.right}) {
+                p->q_parent[c] = i;
+                if (p->nodes[c].left >= 0) ++p->q_pending[i];
+            }
+        }
+        for (size_t t = (size_t)p->stage_begin[0] + p->stage_count[0]; t < p->items.size(); ++t)
+            ++p->q_remaining[p->items[t].node];
+        // [next, status] then live remaining, live pending, parent, initial remaining, initial pending
+        p->queue_bytes = align_up(sizeof(int) * (2 + 5 * (size_t)n_nodes));
+    }
     p->table_offset = p->node_bytes + p->work_bytes + p->leaf_list_bytes;
     p->prec_offset = p->table_offset + p->table_bytes;
     p->crec_offset = p->prec_offset + p->prec_bytes;
-    p->arena_offset = p->crec_offset + p->crec_bytes;
+    p->queue_offset = p->crec_offset + p->crec_bytes;
+    p->arena_offset = p->queue_offset + p->queue_bytes;
     p->arena_bytes = arena;
     p->total_bytes = p->arena_offset + arena;
     p->launches = p->max_height + 1 + (mode == SARBP_SPLIT ? 3 : 0);
@@ -610,6 +630,19 @@ int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_byt
     if (e == cudaSuccess && !plan->leaves.empty())
         e = cudaMemcpyAsync(base + plan->node_bytes + plan->work_bytes, plan->leaves.data(),
                             sizeof(int) * plan->leaves.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && plan->queue_bytes) {
+        const size_t n = (size_t)plan->n_nodes;
+        int* q = reinterpret_cast<int*>(base + plan->queue_offset);
+        e = cudaMemcpyAsync(q + 2 + 2 * n, plan->q_parent.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(q + 2 + 3 * n, plan->q_remaining.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) {
+            std::vector<int> pending = plan->q_pending;
+            if (plan->withheld >= 0) ++pending[plan->withheld];  // never reaches zero
+            e = cudaMemcpyAsync(q + 2 + 4 * n, pending.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // `pending` is a host temporary
+        }
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "FFBP bind: %s", cudaGetErrorString(e));
     plan->bound = workspace;
@@ -629,6 +662,39 @@ int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float
     const cudaError_t e = cudaMemcpyAsync(arena + d.out_offset, image, (size_t)d.nr * d.nu * sizeof(float2),
                                           cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "set_node_image: %s", cudaGetErrorString(e));
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_set_merge_queue(sarbp_ffbp_plan* plan, int on) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (on != 0 && on != 1) return fail(SARBP_ERR_VALUE, "on must be 0 or 1 (got %d)", on);
+    if (on && plan->mode != SARBP_SPLIT) return fail(SARBP_ERR_VALUE, "the merge queue is a split-mode path");
+    plan->merge_queue = on != 0;
+    plan->launches = plan->mode == SARBP_SPLIT
+                         ? 3 + 1 + (plan->max_height > 0 ? (plan->merge_queue ? 1 : plan->max_height) : 0)
+                         : plan->max_height + 1;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_set_wait_limit(sarbp_ffbp_plan* plan, double seconds, int withheld_node) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (!(seconds > 0.0 && seconds <= 60.0)) return fail(SARBP_ERR_VALUE, "the wait limit must be in (0, 60] s");
+    if (withheld_node < -1 || withheld_node >= plan->n_nodes || (withheld_node >= 0 && plan->nodes[withheld_node].left < 0))
+        return fail(SARBP_ERR_VALUE, "withheld_node must be -1 or a merge node");
+    if (plan->bound) return fail(SARBP_ERR_PLAN, "set the wait limit before sarbp_ffbp_bind");
+    plan->queue_limit_ns = (unsigned long long)(seconds * 1e9);
+    plan->withheld = withheld_node;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_status(const sarbp_ffbp_plan* plan, int* status) {
+    if (!plan || !status) return fail(SARBP_ERR_TYPE, "plan and status must not be NULL");
+    if (!plan->bound) return fail(SARBP_ERR_PLAN, "sarbp_ffbp_bind must succeed before status");
+    *status = 0;
+    if (!plan->queue_bytes) return SARBP_OK;
+    const int* q = reinterpret_cast<const int*>(reinterpret_cast<const char*>(plan->bound) + plan->queue_offset);
+    const cudaError_t e = cudaMemcpy(status, q + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "status: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
 
@@ -670,7 +736,24 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
             st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb,
                                           tables, precs, arena, root_out, 0, s);
         const size_t crec_size = split_ffbp_child_record_bytes();
-        for (int h = 1; h <= plan->max_height && st == SARBP_OK; ++h) {
+        if (plan->merge_queue && plan->max_height > 0 && st == SARBP_OK) {
+            const size_t n = (size_t)plan->n_nodes;
+            int* q = reinterpret_cast<int*>(base + plan->queue_offset);
+            cudaError_t e = cudaMemsetAsync(q, 0, 2 * sizeof(int), s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(q + 2, q + 2 + 3 * n, 2 * n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "merge queue reset: %s", cudaGetErrorString(e));
+            MergeQueue Q;
+            Q.next = q;
+            Q.status = q + 1;
+            Q.remaining = q + 2;
+            Q.pending = q + 2 + n;
+            Q.parent = q + 2 + 2 * n;
+            Q.limit_ns = plan->queue_limit_ns;
+            st = launch_split_ffbp_merge_queue(k, nodes, items + plan->stage_begin[1], (int)plan->merge_items, tables,
+                                               crecs, arena, root_out, 0, Q, s);
+        }
+        for (int h = 1; h <= plan->max_height && st == SARBP_OK && !plan->merge_queue; ++h) {
             const size_t first = (size_t)(plan->stage_begin[h] - plan->stage_begin[1]);
             st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables,
                                           reinterpret_cast<char*>(crecs) + 2 * first * crec_size, arena, root_out, 0,

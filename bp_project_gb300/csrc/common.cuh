@@ -265,6 +265,18 @@ size_t split_ffbp_child_record_bytes();
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
                              int chunk, int window_bins, const float4* tables, const void* precs, float2* arena,
                              float2* root_out, int root, cudaStream_t s);
+// Device state of the dependency-counting merge queue (all merge levels in one launch).
+struct MergeQueue {
+    int* next;                    // next item to claim
+    int* remaining;               // per node: tiles not yet written
+    int* pending;                 // per node: merge children not yet complete
+    const int* parent;            // per node: parent index, -1 for the root
+    int* status;                  // 0; 1 once a wait ran out (the image is then incomplete)
+    unsigned long long limit_ns;  // wait limit per item
+};
+int launch_split_ffbp_merge_queue(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
+                                  const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
+                                  const MergeQueue& Q, cudaStream_t s);
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                              const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
                              cudaStream_t s);

@@ -2265,6 +2265,28 @@ __device__ __forceinline__ void child_pair_store(const ChildRec& R, int c, Child
 
 // 4x4 Lagrange stencil of one child at bin (ir, iu) with weights wr (range) and wu (angle);
 // (re, im) run as one f32x2 pair.
+// COHERENT: the child image was written by other CTAs of the same launch (the merge queue), so it
+// is read with weak ld.global (L1-cached, ordered by the acquire that made the node ready) instead
+// of the read-only path.  The asm has no memory clobber, so the compiler schedules it as freely as
+// __ldg; its address comes from values read after the CTA barrier that follows the acquire.
+template <bool COHERENT>
+__device__ __forceinline__ void ld_child_row(const float2* p, float2& x0, float2& x1, float2& x2, float2& x3) {
+    if (COHERENT) {
+        asm("ld.global.v2.f32 {%0, %1}, [%8];\n\t"
+            "ld.global.v2.f32 {%2, %3}, [%8+8];\n\t"
+            "ld.global.v2.f32 {%4, %5}, [%8+16];\n\t"
+            "ld.global.v2.f32 {%6, %7}, [%8+24];"
+            : "=f"(x0.x), "=f"(x0.y), "=f"(x1.x), "=f"(x1.y), "=f"(x2.x), "=f"(x2.y), "=f"(x3.x), "=f"(x3.y)
+            : "l"(p));
+    } else {
+        x0 = __ldg(p);
+        x1 = __ldg(p + 1);
+        x2 = __ldg(p + 2);
+        x3 = __ldg(p + 3);
+    }
+}
+
+template <bool COHERENT>
 __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, int snu, int ir, int iu,
                                                 const float wr[4], const float wu[4]) {
     const float2* base = img + (size_t)(ir - 1) * snu + (iu - 1);
@@ -2272,7 +2294,8 @@ __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, 
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const float2* row = base + (size_t)a * snu;
-        const float2 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2), x3 = __ldg(row + 3);
+        float2 x0, x1, x2, x3;
+        ld_child_row<COHERENT>(row, x0, x1, x2, x3);
         float2 r = __fmul2_rn(pair(wu[0]), x0);
         r = __ffma2_rn(pair(wu[1]), x1, r);
         r = __ffma2_rn(pair(wu[2]), x2, r);
@@ -2287,6 +2310,7 @@ __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, 
 // as packed FP32 pairs.  Both children's phase, sin/cos and bin indices come first, then each
 // child's Lagrange weights just before its stencil, which keeps the live state small enough for
 // two pixels in flight at 40 registers.
+template <bool COHERENT>
 __device__ __forceinline__ float2 child_pair_value(float Kf, const ChildPair& C, const Pix& q) {
     const float2 dx = pair(q.dx), dy = pair(q.dy), nd2 = pair(-q.d2), mone = pair(-1.0f);
     const float2 magic = pair(kMagic), nmagic = pair(-kMagic);
@@ -2334,13 +2358,13 @@ __device__ __forceinline__ float2 child_pair_value(float Kf, const ChildPair& C,
         float wr[4], wu[4];
         lagrange_centred(sr.x, wr);
         lagrange_centred(su.x, wu);
-        v0 = child_stencil(C.img[0], C.snu.x, ir0, iu0, wr, wu);
+        v0 = child_stencil<COHERENT>(C.img[0], C.snu.x, ir0, iu0, wr, wu);
     }
     if (ok1) {
         float wr[4], wu[4];
         lagrange_centred(sr.y, wr);
         lagrange_centred(su.y, wu);
-        v1 = child_stencil(C.img[1], C.snu.y, ir1, iu1, wr, wu);
+        v1 = child_stencil<COHERENT>(C.img[1], C.snu.y, ir1, iu1, wr, wu);
     }
     // (vr cs - vi sn, vr sn + vi cs) per child, then the complex64 sum.
     const float2 o0 = __ffma2_rn(pair(v0.x), make_float2(cs0, sn0), __fmul2_rn(pair(v0.y), make_float2(-sn0, cs0)));
@@ -2350,6 +2374,7 @@ __device__ __forceinline__ float2 child_pair_value(float Kf, const ChildPair& C,
 
 // One merge tile: both children regridded onto the parent tile, each rounded to complex64,
 // then added (the reference's rounding points).  crec points at the tile's two child records.
+template <bool COHERENT = false>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
                                            ChildPair& C, float2* __restrict__ arena, float2* root_out, int root,
@@ -2366,14 +2391,31 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     // One pixel at a time, its offsets read back from the shared tables: little state per
     // thread keeps registers low and more warps resident to hide the child gathers' latency.
     const int cols_t = 1 << J.lc;
+    if (!COHERENT) {
 #pragma unroll 2
-    for (int k = 0; k < kPX; ++k) {
-        const int p = threadIdx.x + kThreads * k;
-        const int row = p >> J.lc, col = p & (cols_t - 1);
-        const Pix v = tab_pixel(T, row, col);
-        const float2 m = child_pair_value(Kf, C, v);
-        const int wr = J.tile_r + row, wu = J.tile_u + col;
-        if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m;
+        for (int k = 0; k < kPX; ++k) {
+            const int p = threadIdx.x + kThreads * k;
+            const int row = p >> J.lc, col = p & (cols_t - 1);
+            const Pix v = tab_pixel(T, row, col);
+            const float2 m = child_pair_value<COHERENT>(Kf, C, v);
+            const int wr = J.tile_r + row, wu = J.tile_u + col;
+            if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m;
+        }
+    } else {
+        // Coherent child loads may not pass this thread's earlier image stores, so the four results
+        // are stored after the last gather.
+        float2 m[kPX];
+#pragma unroll 2
+        for (int k = 0; k < kPX; ++k) {
+            const int p = threadIdx.x + kThreads * k;
+            m[k] = child_pair_value<COHERENT>(Kf, C, tab_pixel(T, p >> J.lc, p & (cols_t - 1)));
+        }
+#pragma unroll
+        for (int k = 0; k < kPX; ++k) {
+            const int p = threadIdx.x + kThreads * k;
+            const int wr = J.tile_r + (p >> J.lc), wu = J.tile_u + (p & (cols_t - 1));
+            if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m[k];
+        }
     }
 }
 
@@ -2388,6 +2430,73 @@ __global__ void __launch_bounds__(kThreads, 6) split_merge_kernel(SplitParams P,
     __shared__ ChildPair C;
     merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, S,
                smem);
+}
+
+// All merge levels in one persistent launch.  Items are in height order; a CTA claims the next
+// item and waits (bounded) until the item's node has no unfinished merge children.  Every
+// dependency of an item has a lower index, so it is held by a running CTA (or finished) and the
+// wait ends.  A finished tile counts down its node's tiles; the node's last tile counts down its
+// parent's pending children.  A wait that runs out sets *status and every CTA stops.
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__global__ void __launch_bounds__(kThreads, 6) split_merge_queue_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+                                                                        const TileItem* __restrict__ items, int nitems,
+                                                                        const float4* __restrict__ tables,
+                                                                        const ChildRec* __restrict__ crecs,
+                                                                        float2* arena, float2* root_out, int root,
+                                                                        MergeQueue Q) {
+    extern __shared__ __align__(16) char smem[];
+    __shared__ TileShared S;
+    __shared__ ChildPair C;
+    __shared__ int s_item, s_ok;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int idx = atomicAdd(Q.next, 1);
+            int ok = 1;
+            if (idx < nitems) {
+                const int node = items[idx].node;
+                const unsigned long long t0 = global_ns();
+                while (ld_acquire_gpu(Q.pending + node) > 0) {
+                    if (ld_acquire_gpu(Q.status) != 0) {  // another CTA gave up: stop too
+                        ok = 0;
+                        break;
+                    }
+                    if (global_ns() - t0 > Q.limit_ns) {
+                        atomicExch(Q.status, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(200);
+                }
+            }
+            s_item = idx;
+            s_ok = ok;
+        }
+        __syncthreads();
+        const int idx = s_item;
+        if (idx >= nitems || !s_ok) return;
+        const TileItem it = items[idx];
+        merge_tile<true>(P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, root_out, root, S, smem);
+        __syncthreads();  // every thread's writes of this tile are issued
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicSub(Q.remaining + it.node, 1) == 1) {
+                __threadfence();
+                const int parent = Q.parent[it.node];
+                if (parent >= 0) atomicSub(Q.pending + parent, 1);
+            }
+        }
+    }
 }
 
 SplitParams make_params(const PulseInputs& in, int chunk, int cap, int pulse_split) {
@@ -2670,6 +2779,30 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
                                                       arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_merges");
+}
+
+int launch_split_ffbp_merge_queue(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
+                                  const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
+                                  const MergeQueue& Q, cudaStream_t s) {
+    if (nitems <= 0) return SARBP_OK;
+    PulseInputs none{};
+    none.k = k;
+    none.data_dr = 1.0;
+    SplitParams P = make_params(none, 1, 4, 1);
+    const size_t smem = merge_smem();
+    if (int st = prepare(split_merge_queue_kernel, smem)) return st;
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, split_merge_queue_kernel, kThreads, smem);
+    if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "merge queue: %s", cudaGetErrorString(e));
+    const int blocks = std::max(1, std::min(nitems, sms * std::max(1, per_sm)));
+    split_merge_queue_kernel<<<blocks, kThreads, smem, s>>>(P, nodes, items, nitems, tables,
+                                                            reinterpret_cast<const ChildRec*>(crecs), arena,
+                                                            root_out, root, Q);
+    note_launches(1);
+    return check_launch("split_ffbp_merge_queue");
 }
 
 // ---- polar image -> ground lattice (evaluate_image on a lattice, split precision) -----------

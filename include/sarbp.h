@@ -338,6 +338,19 @@ int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_byt
  * (bp_project_gb300.shard).  The plan must be bound; the copy is enqueued on `stream` and the plan
  * never writes the node.  No counterpart in the reference (its trees are formed in one process). */
 int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float* image, void* stream);
+/* on = 1: a split plan runs all merge levels as one persistent launch, a dependency-counting queue
+ * in which a parent's tiles start once both its children are complete (no barrier between tree
+ * heights; child images read with coherent loads after an acquire).  on = 0 (the default): one
+ * launch per tree height, which measured faster.  The images are the same bit for bit.  No
+ * counterpart in the reference (its levels are separate launches). */
+int sarbp_ffbp_set_merge_queue(sarbp_ffbp_plan* plan, int on);
+/* The queue's wait limit per merge tile (default 5 s; (0, 60]) and, for tests of that limit, a merge
+ * node whose children are never counted complete (withheld_node >= 0; -1 for none), so that its
+ * tiles' waits run out.  Set before sarbp_ffbp_bind.  A wait that runs out stops the launch and sets
+ * the status read by sarbp_ffbp_status; the image is then incomplete. */
+int sarbp_ffbp_set_wait_limit(sarbp_ffbp_plan* plan, double seconds, int withheld_node);
+/* *status = 1 if a merge-queue wait ran out in the last execute, else 0 (synchronises the device). */
+int sarbp_ffbp_status(const sarbp_ffbp_plan* plan, int* status);
 int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulses, int samples,
                        const double* pos, const double* weight, const double* phase, double range_start,
                        double data_dr, double k, float* out, void* stream);

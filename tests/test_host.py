@@ -100,9 +100,20 @@ def test_ffbp_plan_object_on_host(golden, lib, mode):
     handle = ctypes.c_void_p()
     crop = (plan.crop_r[0], plan.crop_u[0], plan.nr, plan.nu)
     assert h.sarbp_ffbp_plan_create(arr, len(arr), *crop, lib.mode_id(mode), ctypes.byref(handle)) == 0
-    # one launch for all leaves + one per tree height (8 merge levels for 256 leaves),
-    # plus the split path's three prologue launches (geometry tables, leaf pulses, child records)
+    # one launch for all leaves + one per tree height (8 merge levels for 256 leaves); the split path
+    # adds three prologue launches (geometry tables, leaf pulses, child records), and with the merge
+    # queue runs all merges as one launch
     assert h.sarbp_ffbp_launch_count(handle) == (12 if mode == "split" else 9)
+    if mode == "split":
+        assert h.sarbp_ffbp_set_merge_queue(handle, 1) == 0
+        assert h.sarbp_ffbp_launch_count(handle) == 5
+        assert h.sarbp_ffbp_set_merge_queue(handle, 0) == 0
+        assert h.sarbp_ffbp_launch_count(handle) == 12
+        assert h.sarbp_ffbp_set_wait_limit(handle, 0.0, -1) == lib.SARBP_ERR_VALUE
+        assert h.sarbp_ffbp_set_wait_limit(handle, 1.0, len(arr) - 1) == lib.SARBP_ERR_VALUE  # a leaf
+        assert h.sarbp_ffbp_set_wait_limit(handle, 1.0, 0) == 0
+    else:
+        assert h.sarbp_ffbp_set_merge_queue(handle, 1) == lib.SARBP_ERR_VALUE
     ws = h.sarbp_ffbp_workspace_bytes(handle)
     images = sum(n.nr * n.nu * 8 for n in plan.nodes()[1:])
     assert images <= ws <= images * 1.06 + (1 << 26)  # + tables, tile records, node list
