@@ -403,22 +403,6 @@ __device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const floa
     __syncthreads();
 }
 
-// Offsets of tile pixel (row, col) from the tile centre, from the tables (FP32 pairs).
-__device__ __forceinline__ Pix tab_pixel(const TabF& T, int row, int col) {
-    Pix v;
-    v.dxh = T.rxh[row] + T.cxh[col];
-    v.dyh = T.ryh[row] + T.cyh[col];
-    v.dxl = fmaf(T.dg[row], T.dcs[col], T.rxl[row] + T.cxl[col]);
-    v.dyl = fmaf(T.dg[row], T.duu[col], T.ryl[row] + T.cyl[col]);
-    v.dzh = v.dzl = v.dz = 0.0f;
-    v.dx = v.dxh + v.dxl;
-    v.dy = v.dyh + v.dyl;
-    v.d2 = v.dx * v.dx + v.dy * v.dy;
-    v.psi = T.psi[row];
-    v.ar = v.ai = 0.0f;
-    return v;
-}
-
 template <bool HAS_Z>
 __device__ void setup_lattice(const Job& J, TileShared& S, Pix px[kPX]) {
     const sarbp_lattice& L = J.lat;
@@ -2218,11 +2202,11 @@ __device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const
     return make_float2(vr * cs - vi * sn, vr * sn + vi * cs);
 }
 
-// Both child records of a merge tile, each field a (child 0, child 1) pair, so that the two
-// children's coordinate, weight and phase chains run as packed FP32 (f32x2) instructions.
-// Negated copies stand in for the scalar code's subtractions (negation is exact), so every
-// value equals child_value's bit for bit.
-struct __align__(16) ChildPair {
+// Child records of a merge tile for the packed merge: every field of one child as a duplicated
+// (x, x) pair, so that a chain over two parent pixels (the two lanes of f32x2 operations) takes
+// each operand with one 8-byte shared load.  Negated copies stand in for the scalar code's
+// subtractions (negation is exact), so every lane equals child_value's arithmetic bit for bit.
+struct __align__(16) ChildDup {
     float2 nbx, nby;   // -u.x, -u.y
     float2 bz, bw;     // 2 RR, frac(Qr) - 1/2
     float2 ncy, ncz;   // -h.x, -h.y
@@ -2231,36 +2215,56 @@ struct __align__(16) ChildPair {
     float2 nisr, isu;  // -1/sdr, 1/sdu
     float2 ax, ay;     // W_hi.x, W_hi.y
     float2 az, aw;     // W_lo.x, W_lo.y
-    float2 cx, pad;    // Phi
-    int2 ir0, iu0, snr, snu;
-    const float2* img[2];
+    float2 cx;         // Phi
+    int ir0, iu0, snr, snu;
+    const float2* img;
 };
 
-// Thread c in {0, 1} moves child c's record into the pair layout.
-__device__ __forceinline__ void child_pair_store(const ChildRec& R, int c, ChildPair& P) {
-    reinterpret_cast<float*>(&P.nbx)[c] = -R.b.x;
-    reinterpret_cast<float*>(&P.nby)[c] = -R.b.y;
-    reinterpret_cast<float*>(&P.bz)[c] = R.b.z;
-    reinterpret_cast<float*>(&P.bw)[c] = R.b.w;
-    reinterpret_cast<float*>(&P.ncy)[c] = -R.c.y;
-    reinterpret_cast<float*>(&P.ncz)[c] = -R.c.z;
-    reinterpret_cast<float*>(&P.cz)[c] = R.c.z;
-    reinterpret_cast<float*>(&P.cw)[c] = R.c.w;
-    reinterpret_cast<float*>(&P.dx)[c] = R.d.x;
-    reinterpret_cast<float*>(&P.dy)[c] = R.d.y;
-    reinterpret_cast<float*>(&P.nisr)[c] = -R.inv_sdr;
-    reinterpret_cast<float*>(&P.isu)[c] = R.inv_sdu;
-    reinterpret_cast<float*>(&P.ax)[c] = R.a.x;
-    reinterpret_cast<float*>(&P.ay)[c] = R.a.y;
-    reinterpret_cast<float*>(&P.az)[c] = R.a.z;
-    reinterpret_cast<float*>(&P.aw)[c] = R.a.w;
-    reinterpret_cast<float*>(&P.cx)[c] = R.c.x;
-    reinterpret_cast<float*>(&P.pad)[c] = 0.0f;
-    reinterpret_cast<int*>(&P.ir0)[c] = R.ir0;
-    reinterpret_cast<int*>(&P.iu0)[c] = R.iu0;
-    reinterpret_cast<int*>(&P.snr)[c] = R.snr;
-    reinterpret_cast<int*>(&P.snu)[c] = R.snu;
-    P.img[c] = R.img;
+__device__ __forceinline__ void child_dup_store(const ChildRec& R, ChildDup& P) {
+    P.nbx = pair(-R.b.x);
+    P.nby = pair(-R.b.y);
+    P.bz = pair(R.b.z);
+    P.bw = pair(R.b.w);
+    P.ncy = pair(-R.c.y);
+    P.ncz = pair(-R.c.z);
+    P.cz = pair(R.c.z);
+    P.cw = pair(R.c.w);
+    P.dx = pair(R.d.x);
+    P.dy = pair(R.d.y);
+    P.nisr = pair(-R.inv_sdr);
+    P.isu = pair(R.inv_sdu);
+    P.ax = pair(R.a.x);
+    P.ay = pair(R.a.y);
+    P.az = pair(R.a.z);
+    P.aw = pair(R.a.w);
+    P.cx = pair(R.c.x);
+    P.ir0 = R.ir0;
+    P.iu0 = R.iu0;
+    P.snr = R.snr;
+    P.snu = R.snu;
+    P.img = R.img;
+}
+
+// Offsets of the parent pixels (row, col) and (row + 1, col) from the tile centre as (upper,
+// lower) lane pairs, row even: tab_pixel's arithmetic lane by lane, with d2 negated (exact).
+struct VPix {
+    float2 dx, dy, dxh, dyh, dxl, dyl, nd2, psi;
+};
+
+__device__ __forceinline__ float2 ld_pair(const float* p) { return *reinterpret_cast<const float2*>(p); }
+
+__device__ __forceinline__ VPix tab_vpair(const TabF& T, int row, int col) {
+    VPix v;
+    v.dxh = __fadd2_rn(ld_pair(T.rxh + row), pair(T.cxh[col]));  // exact: both multiples of the quantum
+    v.dyh = __fadd2_rn(ld_pair(T.ryh + row), pair(T.cyh[col]));
+    const float2 dg = ld_pair(T.dg + row);
+    v.dxl = __ffma2_rn(dg, pair(T.dcs[col]), __fadd2_rn(ld_pair(T.rxl + row), pair(T.cxl[col])));
+    v.dyl = __ffma2_rn(dg, pair(T.duu[col]), __fadd2_rn(ld_pair(T.ryl + row), pair(T.cyl[col])));
+    v.dx = __fadd2_rn(v.dxh, v.dxl);
+    v.dy = __fadd2_rn(v.dyh, v.dyl);
+    v.nd2 = __fmul2_rn(__ffma2_rn(v.dx, v.dx, __fmul2_rn(v.dy, v.dy)), pair(-1.0f));
+    v.psi = ld_pair(T.psi + row);
+    return v;
 }
 
 // 4x4 Lagrange stencil of one child at bin (ir, iu) with weights wr (range) and wu (angle);
@@ -2305,121 +2309,155 @@ __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, 
     return v;
 }
 
-// The parent pixel q from both children: child_value(C0, q) + child_value(C1, q) (each child
-// rounded to complex64, then the FP32 add) with the two children's coordinate and phase chains
-// as packed FP32 pairs.  Both children's phase, sin/cos and bin indices come first, then each
-// child's Lagrange weights just before its stencil, which keeps the live state small enough for
-// two pixels in flight at 40 registers.
+// Child C at the column pair q (lanes: the upper and the lower parent pixel), rotated: per lane
+// child_value's arithmetic (the Lagrange weights, the stencil's sum order and the rotation are
+// the same).  Two vertically adjacent parent pixels nearly always fall one child range bin apart
+// in the same angle column (a parent range step is one child range step, shortened by the
+// cosine of the angle between the two phase centres' lines of sight), so their 4x4 stencils
+// share three rows: when that holds for every lane of the warp, the pair gathers one 5x4 block
+// (20 loads instead of 32).  Otherwise each pixel gathers its own stencil.
 template <bool COHERENT>
-__device__ __forceinline__ float2 child_pair_value(float Kf, const ChildPair& C, const Pix& q) {
-    const float2 dx = pair(q.dx), dy = pair(q.dy), nd2 = pair(-q.d2), mone = pair(-1.0f);
-    const float2 magic = pair(kMagic), nmagic = pair(-kMagic);
-    const float2 nL = __ffma2_rn(C.nbx, dx, __fmul2_rn(C.nby, dy));
-    const float2 nq2 = __ffma2_rn(nL, nL, nd2);
+__device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const VPix& q, float2& oA, float2& oB) {
+    const float2 magic = pair(kMagic), nmagic = pair(-kMagic), mone = pair(-1.0f);
+    const float2 nL = __ffma2_rn(C.nbx, q.dx, __fmul2_rn(C.nby, q.dy));
+    const float2 nq2 = __ffma2_rn(nL, nL, q.nd2);
     const float2 den = __ffma2_rn(pair(-2.0f), nL, C.bz);
     const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
     const float2 ne0 = __fmul2_rn(nq2, B);
     const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);
-    // Phase (turns) first, so that the pixel's offsets die before the stencils.
-    const float2 tb = __ffma2_rn(C.ax, pair(q.dxh), __fmul2_rn(C.ay, pair(q.dyh)));
+    const float2 tb = __ffma2_rn(C.ax, q.dxh, __fmul2_rn(C.ay, q.dyh));
     float2 sm = __ffma2_rn(pair(-Kf), neps, C.cx);
-    sm = __ffma2_rn(C.ax, pair(q.dxl), sm);
-    sm = __ffma2_rn(C.ay, pair(q.dyl), sm);
-    sm = __ffma2_rn(C.az, dx, sm);
-    sm = __ffma2_rn(C.aw, dy, sm);
+    sm = __ffma2_rn(C.ax, q.dxl, sm);
+    sm = __ffma2_rn(C.ay, q.dyl, sm);
+    sm = __ffma2_rn(C.az, q.dx, sm);
+    sm = __ffma2_rn(C.aw, q.dy, sm);
     const float2 rtb = __fadd2_rn(__fadd2_rn(tb, magic), nmagic);
-    const float2 tot = __fadd2_rn(__ffma2_rn(rtb, mone, tb), __fadd2_rn(sm, pair(q.psi)));
+    const float2 tot = __fadd2_rn(__ffma2_rn(rtb, mone, tb), __fadd2_rn(sm, q.psi));
     const float2 rtot = __fadd2_rn(__fadd2_rn(tot, magic), nmagic);
     const float2 ang = __fmul2_rn(__ffma2_rn(rtot, mone, tot), pair(kTwoPiF));
-    float sn0, cs0, sn1, cs1;
-    __sincosf(ang.x, &sn0, &cs0);
-    __sincosf(ang.y, &sn1, &cs1);
+    float snA, csA, snB, csB;
+    __sincosf(ang.x, &snA, &csA);
+    __sincosf(ang.y, &snB, &csB);
     const float2 qr = __ffma2_rn(__fadd2_rn(nL, neps), C.nisr, C.bw);
     const float2 tr = __fadd2_rn(qr, magic);
     const float2 sr = __ffma2_rn(__fadd2_rn(tr, nmagic), mone, qr);
-    const float2 nLh = __ffma2_rn(C.ncy, dx, __fmul2_rn(C.ncz, dy));
-    const float2 nq2h = __ffma2_rn(nLh, nLh, nd2);
+    const float2 nLh = __ffma2_rn(C.ncy, q.dx, __fmul2_rn(C.ncz, q.dy));
+    const float2 nq2h = __ffma2_rn(nLh, nLh, q.nd2);
     const float2 denh = __ffma2_rn(pair(-2.0f), nLh, C.cw);
     const float2 Bh = make_float2(rcp_approx(denh.x), rcp_approx(denh.y));
     const float2 neh = __fmul2_rn(nq2h, Bh);
     const float2 ndG = __fadd2_rn(nLh, __ffma2_rn(__fmul2_rn(neh, neh), Bh, neh));
     const float2 gp = __ffma2_rn(ndG, mone, C.dx);
-    const float2 num = __ffma2_rn(C.cz, ndG, dy);
+    const float2 num = __ffma2_rn(C.cz, ndG, q.dy);
     const float2 duu = __fmul2_rn(num, make_float2(rcp_approx(gp.x), rcp_approx(gp.y)));
     const float2 qu = __ffma2_rn(duu, C.isu, C.dy);
     const float2 tu = __fadd2_rn(qu, magic);
     const float2 su = __ffma2_rn(__fadd2_rn(tu, nmagic), mone, qu);
-    const int ir0 = C.ir0.x + (__float_as_int(tr.x) - kMagicBits), ir1 = C.ir0.y + (__float_as_int(tr.y) - kMagicBits);
-    const int iu0 = C.iu0.x + (__float_as_int(tu.x) - kMagicBits), iu1 = C.iu0.y + (__float_as_int(tu.y) - kMagicBits);
-    const bool ok0 = ir0 >= 1 && ir0 <= C.snr.x - 3 && iu0 >= 1 && iu0 <= C.snu.x - 3 && gp.x > 0.0f;
-    const bool ok1 = ir1 >= 1 && ir1 <= C.snr.y - 3 && iu1 >= 1 && iu1 <= C.snu.y - 3 && gp.y > 0.0f;
-    float2 v0 = make_float2(0.0f, 0.0f), v1 = v0;
-    if (ok0) {
-        float wr[4], wu[4];
-        lagrange_centred(sr.x, wr);
-        lagrange_centred(su.x, wu);
-        v0 = child_stencil<COHERENT>(C.img[0], C.snu.x, ir0, iu0, wr, wu);
+    const int irA = C.ir0 + (__float_as_int(tr.x) - kMagicBits), irB = C.ir0 + (__float_as_int(tr.y) - kMagicBits);
+    const int iuA = C.iu0 + (__float_as_int(tu.x) - kMagicBits), iuB = C.iu0 + (__float_as_int(tu.y) - kMagicBits);
+    const bool okA = irA >= 1 && irA <= C.snr - 3 && iuA >= 1 && iuA <= C.snu - 3 && gp.x > 0.0f;
+    const bool okB = irB >= 1 && irB <= C.snr - 3 && iuB >= 1 && iuB <= C.snu - 3 && gp.y > 0.0f;
+    float2 vA = make_float2(0.0f, 0.0f), vB = vA;
+    if (__all_sync(0xffffffffu, okA && okB && irB == irA + 1 && iuB == iuA)) {
+        float wrA[4], wuA[4], wrB[4], wuB[4];
+        lagrange_centred(sr.x, wrA);
+        lagrange_centred(su.x, wuA);
+        lagrange_centred(sr.y, wrB);
+        lagrange_centred(su.y, wuB);
+        const float2* row = C.img + (size_t)(irA - 1) * C.snu + (iuA - 1);
+#pragma unroll
+        for (int a = 0; a < 5; ++a) {
+            float2 x0, x1, x2, x3;
+            ld_child_row<COHERENT>(row + (size_t)a * C.snu, x0, x1, x2, x3);
+            if (a < 4) {
+                float2 r = __fmul2_rn(pair(wuA[0]), x0);
+                r = __ffma2_rn(pair(wuA[1]), x1, r);
+                r = __ffma2_rn(pair(wuA[2]), x2, r);
+                r = __ffma2_rn(pair(wuA[3]), x3, r);
+                vA = __ffma2_rn(pair(wrA[a]), r, vA);
+            }
+            if (a > 0) {
+                float2 r = __fmul2_rn(pair(wuB[0]), x0);
+                r = __ffma2_rn(pair(wuB[1]), x1, r);
+                r = __ffma2_rn(pair(wuB[2]), x2, r);
+                r = __ffma2_rn(pair(wuB[3]), x3, r);
+                vB = __ffma2_rn(pair(wrB[a - 1]), r, vB);
+            }
+        }
+    } else {
+        if (okA) {
+            float wr[4], wu[4];
+            lagrange_centred(sr.x, wr);
+            lagrange_centred(su.x, wu);
+            vA = child_stencil<COHERENT>(C.img, C.snu, irA, iuA, wr, wu);
+        }
+        if (okB) {
+            float wr[4], wu[4];
+            lagrange_centred(sr.y, wr);
+            lagrange_centred(su.y, wu);
+            vB = child_stencil<COHERENT>(C.img, C.snu, irB, iuB, wr, wu);
+        }
     }
-    if (ok1) {
-        float wr[4], wu[4];
-        lagrange_centred(sr.y, wr);
-        lagrange_centred(su.y, wu);
-        v1 = child_stencil<COHERENT>(C.img[1], C.snu.y, ir1, iu1, wr, wu);
-    }
-    // (vr cs - vi sn, vr sn + vi cs) per child, then the complex64 sum.
-    const float2 o0 = __ffma2_rn(pair(v0.x), make_float2(cs0, sn0), __fmul2_rn(pair(v0.y), make_float2(-sn0, cs0)));
-    const float2 o1 = __ffma2_rn(pair(v1.x), make_float2(cs1, sn1), __fmul2_rn(pair(v1.y), make_float2(-sn1, cs1)));
-    return __fadd2_rn(o0, o1);
+    // (vr cs - vi sn, vr sn + vi cs)
+    oA = __ffma2_rn(pair(vA.x), make_float2(csA, snA), __fmul2_rn(pair(vA.y), make_float2(-snA, csA)));
+    oB = __ffma2_rn(pair(vB.x), make_float2(csB, snB), __fmul2_rn(pair(vB.y), make_float2(-snB, csB)));
 }
 
 // One merge tile: both children regridded onto the parent tile, each rounded to complex64,
 // then added (the reference's rounding points).  crec points at the tile's two child records.
+// Thread t forms the column pairs (rows 2 m and 2 m + 1 of column t mod cols) for
+// m = t / cols and m + 256 / cols; its offsets come back from the shared tables per pair, which
+// keeps the live state small.
 template <bool COHERENT = false>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
-                                           ChildPair& C, float2* __restrict__ arena, float2* root_out, int root,
+                                           ChildDup* C, float2* __restrict__ arena, float2* root_out, int root,
                                            TileShared& S, char* smem) {
     Job J;
     J.g = nodes[it.node];
     J.lc = J.g.tile_lc;
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
-    if (threadIdx.x < 2) child_pair_store(crec[threadIdx.x], threadIdx.x, C);
+    if (threadIdx.x < 2) child_dup_store(crec[threadIdx.x], C[threadIdx.x]);
     TabF& T = *reinterpret_cast<TabF*>(smem);
     setup_polar_tab(J, S, T, tables);
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
-    // One pixel at a time, its offsets read back from the shared tables: little state per
-    // thread keeps registers low and more warps resident to hide the child gathers' latency.
-    const int cols_t = 1 << J.lc;
-    if (!COHERENT) {
-#pragma unroll 2
-        for (int k = 0; k < kPX; ++k) {
-            const int p = threadIdx.x + kThreads * k;
-            const int row = p >> J.lc, col = p & (cols_t - 1);
-            const Pix v = tab_pixel(T, row, col);
-            const float2 m = child_pair_value<COHERENT>(Kf, C, v);
-            const int wr = J.tile_r + row, wu = J.tile_u + col;
-            if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m;
-        }
-    } else {
-        // Coherent child loads may not pass this thread's earlier image stores, so the four results
-        // are stored after the last gather.
-        float2 m[kPX];
-#pragma unroll 2
-        for (int k = 0; k < kPX; ++k) {
-            const int p = threadIdx.x + kThreads * k;
-            m[k] = child_pair_value<COHERENT>(Kf, C, tab_pixel(T, p >> J.lc, p & (cols_t - 1)));
-        }
+    const int col = threadIdx.x & ((1 << J.lc) - 1), wu = J.tile_u + col;
+    float2 m[kPX];
 #pragma unroll
-        for (int k = 0; k < kPX; ++k) {
-            const int p = threadIdx.x + kThreads * k;
-            const int wr = J.tile_r + (p >> J.lc), wu = J.tile_u + (p & (cols_t - 1));
-            if (wr < J.g.win_nr && wu < J.g.win_nu) dst[(long long)wr * J.g.out_stride + wu] = m[k];
+    for (int k = 0; k < kPX / 2; ++k) {
+        const int row = 2 * ((threadIdx.x >> J.lc) + (kThreads >> J.lc) * k);
+        const VPix v = tab_vpair(T, row, col);
+        float2 a0, b0, a1, b1;
+        child_vpair<COHERENT>(Kf, C[0], v, a0, b0);
+        child_vpair<COHERENT>(Kf, C[1], v, a1, b1);
+        const float2 mA = __fadd2_rn(a0, a1), mB = __fadd2_rn(b0, b1);
+        if (!COHERENT) {
+            const int wr = J.tile_r + row;
+            if (wu < J.g.win_nu) {
+                if (wr < J.g.win_nr) dst[(long long)wr * J.g.out_stride + wu] = mA;
+                if (wr + 1 < J.g.win_nr) dst[(long long)(wr + 1) * J.g.out_stride + wu] = mB;
+            }
+        } else {
+            // Coherent child loads may not pass this thread's earlier image stores, so the
+            // results are stored after the last gather.
+            m[2 * k] = mA;
+            m[2 * k + 1] = mB;
+        }
+    }
+    if (COHERENT) {
+#pragma unroll
+        for (int k = 0; k < kPX / 2; ++k) {
+            const int wr = J.tile_r + 2 * ((threadIdx.x >> J.lc) + (kThreads >> J.lc) * k);
+            if (wu < J.g.win_nu) {
+                if (wr < J.g.win_nr) dst[(long long)wr * J.g.out_stride + wu] = m[2 * k];
+                if (wr + 1 < J.g.win_nr) dst[(long long)(wr + 1) * J.g.out_stride + wu] = m[2 * k + 1];
+            }
         }
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 6) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kThreads, 5) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
                                                                   const float4* __restrict__ tables,
                                                                   const ChildRec* __restrict__ crecs,
@@ -2427,7 +2465,7 @@ __global__ void __launch_bounds__(kThreads, 6) split_merge_kernel(SplitParams P,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ ChildPair C;
+    __shared__ ChildDup C[2];
     merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, S,
                smem);
 }
@@ -2449,7 +2487,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-__global__ void __launch_bounds__(kThreads, 6) split_merge_queue_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kThreads, 4) split_merge_queue_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                         const TileItem* __restrict__ items, int nitems,
                                                                         const float4* __restrict__ tables,
                                                                         const ChildRec* __restrict__ crecs,
@@ -2457,7 +2495,7 @@ __global__ void __launch_bounds__(kThreads, 6) split_merge_queue_kernel(SplitPar
                                                                         MergeQueue Q) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ ChildPair C;
+    __shared__ ChildDup C[2];
     __shared__ int s_item, s_ok;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -2944,7 +2982,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_leaf_kernel(const BatchScen
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchScene* __restrict__ scenes,
+__global__ void __launch_bounds__(kThreads, 5) batch_merge_kernel(const BatchScene* __restrict__ scenes,
                                                                   const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items, int nitems,
                                                                   const float4* __restrict__ tables,
@@ -2953,7 +2991,7 @@ __global__ void __launch_bounds__(kThreads, 6) batch_merge_kernel(const BatchSce
                                                                   unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
     __shared__ TileShared S;
-    __shared__ ChildPair C;
+    __shared__ ChildDup C[2];
     __shared__ int s_item;
     for (;;) {
         const int idx = next_item(counter, s_item);
