@@ -332,73 +332,122 @@ __device__ __forceinline__ void quantize_pair(float& p, float& e, float q, float
     p = h;
 }
 
-__device__ void setup_polar_tab(const Job& J, TileShared& S, TabF& T, const float4* __restrict__ tables) {
+// One row (i) and one column (j) of a merge tile's tables, before quantization; r0v and c0v are
+// the tile centre's row and column (i0, j0).
+struct TabRow {
+    float rxh, rxl, ryh, ryl, dg, psi;
+};
+struct TabCol {
+    float cxh, cxl, cyh, cyl, dcs, duu;
+};
+
+__device__ __forceinline__ TabRow tab_row(const PolarDesc& g, const float4* __restrict__ tables, float4 r0v,
+                                          float4 c0v, int i) {
+    const float4 rv = __ldg(tables + g.rows_off + 3 * (long long)i);
+    const float side = (float)g.side;
+    const float dh = rv.x - r0v.x, dl = rv.y - r0v.y;  // g values of one node: dh is exact
+    TabRow R;
+    float p, e;
+    two_prod(dh, dl, c0v.x, c0v.y, p, e);
+    R.rxh = side * p;
+    R.rxl = side * e;
+    two_prod(dh, dl, c0v.z, c0v.w, p, e);
+    R.ryh = p;
+    R.ryl = e;
+    R.dg = dh + dl;
+    R.psi = rv.z;
+    return R;
+}
+
+__device__ __forceinline__ TabCol tab_col(const PolarDesc& g, const float4* __restrict__ tables, float4 r0v,
+                                          float4 c0v, int j, int j0) {
+    const float4 cv = __ldg(tables + g.cols_off + j);
+    const float side = (float)g.side;
+    const float ch = cv.x - c0v.x, cl = cv.y - c0v.y;  // c in (0, 1] within a factor 2: exact
+    // u_j - u_0 = (j - j0) du, formed from the integer offset (no cancellation).
+    const float kj = (float)(j - j0);
+    const float duh = (float)g.du, dul = (float)(g.du - (double)duh);
+    const float uh = kj * duh;
+    const float ul = fmaf(kj, duh, -uh) + kj * dul;
+    TabCol C;
+    float p, e;
+    two_prod(r0v.x, r0v.y, ch, cl, p, e);
+    C.cxh = side * p;
+    C.cxl = side * e;
+    two_prod(r0v.x, r0v.y, uh, ul, p, e);
+    C.cyh = p;
+    C.cyl = e;
+    C.dcs = side * (ch + cl);
+    C.duu = uh + ul;
+    return C;
+}
+
+// Tile centre row and column of a merge tile (rows_t x cols_t pixels at (tile_r, tile_u)).
+__device__ __forceinline__ void tab_centre(const PolarDesc& g, int lc, int tile_r, int tile_u,
+                                           const float4* __restrict__ tables, float4& r0v, float4& c0v, int& j0) {
+    const int cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
+    const int i0 = min(g.win_r0 + tile_r + (rows_t >> 1), g.nr - 1);
+    j0 = min(g.win_u0 + tile_u + (cols_t >> 1), g.nu - 1);
+    r0v = __ldg(tables + g.rows_off + 3 * (long long)i0);
+    c0v = __ldg(tables + g.cols_off + j0);
+}
+
+// Power-of-two quantum of a merge tile's pixel offsets, 2^(e - 12) with the bound on |delta_x|,
+// |delta_y| = m 2^e, m in [0.5, 1): row terms are monotone in i and column terms extreme at the
+// tile edges, so the bound comes from the first and last row and column.  FP32 bit arithmetic;
+// computed once per tile in the child-record prologue.
+__device__ __forceinline__ void tab_quantum(const PolarDesc& g, int lc, int tile_r, int tile_u,
+                                            const float4* __restrict__ tables, float& q, float& iq) {
+    const int cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
+    float4 r0v, c0v;
+    int j0;
+    tab_centre(g, lc, tile_r, tile_u, tables, r0v, c0v, j0);
+    const TabRow ra = tab_row(g, tables, r0v, c0v, min(g.win_r0 + tile_r, g.nr - 1));
+    const TabRow rb = tab_row(g, tables, r0v, c0v, min(g.win_r0 + tile_r + rows_t - 1, g.nr - 1));
+    const TabCol ca = tab_col(g, tables, r0v, c0v, min(g.win_u0 + tile_u, g.nu - 1), j0);
+    const TabCol cb = tab_col(g, tables, r0v, c0v, min(g.win_u0 + tile_u + cols_t - 1, g.nu - 1), j0);
+    const float mrx = fmaxf(fabsf(ra.rxh), fabsf(rb.rxh)), mry = fmaxf(fabsf(ra.ryh), fabsf(rb.ryh));
+    const float mdg = fmaxf(fabsf(ra.dg), fabsf(rb.dg));
+    const float mcx = fmaxf(fabsf(ca.cxh), fabsf(cb.cxh)), mcy = fmaxf(fabsf(ca.cyh), fabsf(cb.cyh));
+    const float mdc = fmaxf(fabsf(ca.dcs), fabsf(cb.dcs)), mdu = fmaxf(fabsf(ca.duu), fabsf(cb.duu));
+    const float bx = fmaf(fmaf(mdg, mdc, mrx + mcx), 1.0001f, 1e-6f);
+    const float by = fmaf(fmaf(mdg, mdu, mry + mcy), 1.0001f, 1e-6f);
+    const int e = ((__float_as_int(fmaxf(bx, by)) >> 23) & 0xff) - 126;
+    q = __int_as_float((e - 12 + 127) << 23);
+    iq = __int_as_float((12 - e + 127) << 23);
+}
+
+// Polar merge-tile set-up from per-node tables of float pairs (FFBP): FP32 two-float arithmetic
+// only, one barrier.  The offsets are quantized on the tile's quantum (q, iq) from its child
+// record, so each table entry is final when it is written.
+__device__ void setup_polar_tab(const Job& J, TabF& T, const float4* __restrict__ tables, float q, float iq) {
     const PolarDesc& g = J.g;
     const int tid = threadIdx.x;
     const int cols_t = 1 << J.lc, rows_t = kSplitTilePixels >> J.lc;
-    const int i0 = min(g.win_r0 + J.tile_r + (rows_t >> 1), g.nr - 1);
-    const int j0 = min(g.win_u0 + J.tile_u + (cols_t >> 1), g.nu - 1);
-    const float4 r0v = __ldg(tables + g.rows_off + 3 * (long long)i0);
-    const float4 c0v = __ldg(tables + g.cols_off + j0);
-    const float side = (float)g.side;
+    float4 r0v, c0v;
+    int j0;
+    tab_centre(g, J.lc, J.tile_r, J.tile_u, tables, r0v, c0v, j0);
     if (tid < rows_t) {
-        const int i = min(g.win_r0 + J.tile_r + tid, g.nr - 1);
-        const float4 rv = __ldg(tables + g.rows_off + 3 * (long long)i);
-        const float dh = rv.x - r0v.x, dl = rv.y - r0v.y;  // g values of one node: dh is exact
-        float p, e;
-        two_prod(dh, dl, c0v.x, c0v.y, p, e);
-        T.rxh[tid] = side * p;
-        T.rxl[tid] = side * e;
-        two_prod(dh, dl, c0v.z, c0v.w, p, e);
-        T.ryh[tid] = p;
-        T.ryl[tid] = e;
-        T.dg[tid] = dh + dl;
-        T.psi[tid] = rv.z;
+        TabRow R = tab_row(g, tables, r0v, c0v, min(g.win_r0 + J.tile_r + tid, g.nr - 1));
+        quantize_pair(R.rxh, R.rxl, q, iq);
+        quantize_pair(R.ryh, R.ryl, q, iq);
+        T.rxh[tid] = R.rxh;
+        T.rxl[tid] = R.rxl;
+        T.ryh[tid] = R.ryh;
+        T.ryl[tid] = R.ryl;
+        T.dg[tid] = R.dg;
+        T.psi[tid] = R.psi;
     }
     if (tid < cols_t) {
-        const int j = min(g.win_u0 + J.tile_u + tid, g.nu - 1);
-        const float4 cv = __ldg(tables + g.cols_off + j);
-        const float ch = cv.x - c0v.x, cl = cv.y - c0v.y;  // c in (0, 1] within a factor 2: exact
-        // u_j - u_0 = (j - j0) du, formed from the integer offset (no cancellation).
-        const float kj = (float)(j - j0);
-        const float duh = (float)g.du, dul = (float)(g.du - (double)duh);
-        const float uh = kj * duh;
-        const float ul = fmaf(kj, duh, -uh) + kj * dul;
-        float p, e;
-        two_prod(r0v.x, r0v.y, ch, cl, p, e);
-        T.cxh[tid] = side * p;
-        T.cxl[tid] = side * e;
-        two_prod(r0v.x, r0v.y, uh, ul, p, e);
-        T.cyh[tid] = p;
-        T.cyl[tid] = e;
-        T.dcs[tid] = side * (ch + cl);
-        T.duu[tid] = uh + ul;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        // Row terms are monotone in i and column terms extreme at the tile edges.
-        const int rl = rows_t - 1, cl = cols_t - 1;
-        const float mrx = fmaxf(fabsf(T.rxh[0]), fabsf(T.rxh[rl])), mry = fmaxf(fabsf(T.ryh[0]), fabsf(T.ryh[rl]));
-        const float mdg = fmaxf(fabsf(T.dg[0]), fabsf(T.dg[rl]));
-        const float mcx = fmaxf(fabsf(T.cxh[0]), fabsf(T.cxh[cl])), mcy = fmaxf(fabsf(T.cyh[0]), fabsf(T.cyh[cl]));
-        const float mdc = fmaxf(fabsf(T.dcs[0]), fabsf(T.dcs[cl])), mdu = fmaxf(fabsf(T.duu[0]), fabsf(T.duu[cl]));
-        const float bx = (mrx + mcx + mdg * mdc) * 1.0001f + 1e-6f;
-        const float by = (mry + mcy + mdg * mdu) * 1.0001f + 1e-6f;
-        // Power-of-two quantum 2^(e - 12) with bound = m 2^e, m in [0.5, 1): FP32 bit arithmetic,
-        // no FP64 in this serial section (merges use only the quantum from the tile set-up).
-        const int e = ((__float_as_int(fmaxf(bx, by)) >> 23) & 0xff) - 126;
-        S.scale_f = __int_as_float((e - 12 + 127) << 23);
-        S.inv_scale_f = __int_as_float((12 - e + 127) << 23);
-    }
-    __syncthreads();
-    const float q = S.scale_f, iq = S.inv_scale_f;
-    if (tid < rows_t) {
-        quantize_pair(T.rxh[tid], T.rxl[tid], q, iq);
-        quantize_pair(T.ryh[tid], T.ryl[tid], q, iq);
-    }
-    if (tid < cols_t) {
-        quantize_pair(T.cxh[tid], T.cxl[tid], q, iq);
-        quantize_pair(T.cyh[tid], T.cyl[tid], q, iq);
+        TabCol C = tab_col(g, tables, r0v, c0v, min(g.win_u0 + J.tile_u + tid, g.nu - 1), j0);
+        quantize_pair(C.cxh, C.cxl, q, iq);
+        quantize_pair(C.cyh, C.cyl, q, iq);
+        T.cxh[tid] = C.cxh;
+        T.cxl[tid] = C.cxl;
+        T.cyh[tid] = C.cyh;
+        T.cyl[tid] = C.cyl;
+        T.dcs[tid] = C.dcs;
+        T.duu[tid] = C.duu;
     }
     __syncthreads();
 }
@@ -2120,7 +2169,9 @@ __device__ __forceinline__ void child_record(FF K, float scale_w, float inv_scal
     const FF gc = ff_mul(g0, FF{cv.x, cv.y});
     const FF px = ff_add(ff_of(g.tf[0]), g.side < 0 ? ff_neg(gc) : gc);
     const FF py = ff_add(ff_of(g.tf[1]), ff_mul(g0, FF{cv.z, cv.w}));
-    out[t] = child_rec_at(K, scale_w, inv_scale_w, c, px, py, arena + c.out_offset);
+    ChildRec R = child_rec_at(K, scale_w, inv_scale_w, c, px, py, arena + c.out_offset);
+    if (!(t & 1)) tab_quantum(g, g.tile_lc, it.tile_r, it.tile_u, tables, R.d.z, R.d.w);
+    out[t] = R;
 }
 
 __global__ void ffbp_child_records_kernel(float Kh, float Kl, float scale_w, float inv_scale_w,
@@ -2412,15 +2463,16 @@ template <bool COHERENT = false>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
                                            ChildDup* C, float2* __restrict__ arena, float2* root_out, int root,
-                                           TileShared& S, char* smem) {
+                                           char* smem) {
     Job J;
     J.g = nodes[it.node];
     J.lc = J.g.tile_lc;
     J.tile_r = it.tile_r;
     J.tile_u = it.tile_u;
     if (threadIdx.x < 2) child_dup_store(crec[threadIdx.x], C[threadIdx.x]);
+    const float4 d0 = __ldg(&crec[0].d);  // (G, frac(Qu) - 1/2, tile quantum, its inverse)
     TabF& T = *reinterpret_cast<TabF*>(smem);
-    setup_polar_tab(J, S, T, tables);
+    setup_polar_tab(J, T, tables, d0.z, d0.w);
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
     const int col = threadIdx.x & ((1 << J.lc) - 1), wu = J.tile_u + col;
     float2 m[kPX];
@@ -2464,10 +2516,8 @@ __global__ void __launch_bounds__(kThreads, 5) split_merge_kernel(SplitParams P,
                                                                   float2* __restrict__ arena, float2* root_out,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
-    __shared__ TileShared S;
     __shared__ ChildDup C[2];
-    merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, S,
-               smem);
+    merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, smem);
 }
 
 // All merge levels in one persistent launch.  Items are in height order; a CTA claims the next
@@ -2494,7 +2544,6 @@ __global__ void __launch_bounds__(kThreads, 4) split_merge_queue_kernel(SplitPar
                                                                         float2* arena, float2* root_out, int root,
                                                                         MergeQueue Q) {
     extern __shared__ __align__(16) char smem[];
-    __shared__ TileShared S;
     __shared__ ChildDup C[2];
     __shared__ int s_item, s_ok;
     for (;;) {
@@ -2524,7 +2573,7 @@ __global__ void __launch_bounds__(kThreads, 4) split_merge_queue_kernel(SplitPar
         const int idx = s_item;
         if (idx >= nitems || !s_ok) return;
         const TileItem it = items[idx];
-        merge_tile<true>(P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, root_out, root, S, smem);
+        merge_tile<true>(P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, root_out, root, smem);
         __syncthreads();  // every thread's writes of this tile are issued
         if (threadIdx.x == 0) {
             __threadfence();
@@ -2990,14 +3039,13 @@ __global__ void __launch_bounds__(kThreads, 5) batch_merge_kernel(const BatchSce
                                                                   float2* __restrict__ arena, int* counter,
                                                                   unsigned long long* trace) {
     extern __shared__ __align__(16) char smem[];
-    __shared__ TileShared S;
     __shared__ ChildDup C[2];
     __shared__ int s_item;
     for (;;) {
         const int idx = next_item(counter, s_item);
         if (idx >= nitems) return;
         const TileItem it = items[idx];
-        merge_tile(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, nullptr, -1, S, smem);
+        merge_tile(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, nullptr, -1, smem);
         trace_item(trace, it.pad);
     }
 }
