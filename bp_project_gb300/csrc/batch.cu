@@ -175,9 +175,7 @@ int sarbp_batch_create(const sarbp_batch_scene* scenes, int n_scenes, int blocks
             }
             for (int leaf : p->leaves) b->leaves.push_back(leaf + node0);
             // Leaf window and chunk exactly as sarbp_ffbp_execute chooses them.
-            double span = 0.0;
-            for (int leaf : p->leaves) span = std::max(span, 32.0 * fabs(p->nodes[leaf].dr));
-            d.window_bins = (int)ceil(span / fabs(s.data_dr)) + 48;
+            d.window_bins = (int)ceil(ffbp_leaf_tile_span(*p) / fabs(s.data_dr)) + 48;
             d.chunk = split_chunk_for(d.window_bins, s.chunk_pulses ? s.chunk_pulses : p->leaf_chunk, true);
             d.prec_offset = b->pulse_records;
             for (int t = p->stage_begin[0]; t < p->stage_begin[0] + p->stage_count[0]; ++t) {

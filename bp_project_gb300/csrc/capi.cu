@@ -527,9 +527,19 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         if (d.left >= 0 && mode == SARBP_SPLIT) d.tile_lc = split_polar_tile_lc_slack(d, kMergeTileSlack, nullptr);
         const bool external = d.left < 0 && d.a < 0;
         if (d.left < 0 && mode == SARBP_SPLIT && !external) {
-            // Leaves use the origin formulation: precision does not depend on the tile shape, and
-            // 32-row tiles keep each pulse's range window short.
+            // Leaves use the origin formulation: precision does not depend on the tile shape.  Of the
+            // 32x32, 16x64 and 8x128 shapes the one with the fewest tiles over the leaf grid wastes the
+            // least work on pixels past its edge (ties: the shorter tile, whose range windows are shorter).
             d.tile_lc = 5;
+            long long fewest = -1;
+            for (int lc = 5; lc >= 3; --lc) {
+                const long long rows_t = kSplitTilePixels >> lc, cols_t = 1LL << lc;
+                const long long t = ((d.win_nr + rows_t - 1) / rows_t) * ((d.win_nu + cols_t - 1) / cols_t);
+                if (fewest < 0 || t < fewest) {
+                    fewest = t;
+                    d.tile_lc = lc;
+                }
+            }
             p->leaves.push_back(i);
             p->max_pulse = std::max(p->max_pulse, d.b);
         }
@@ -721,10 +731,8 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
         float4* tables = reinterpret_cast<float4*>(base + plan->table_offset);
         void* precs = base + plan->prec_offset;
         void* crecs = base + plan->crec_offset;
-        // A 32-row leaf tile spans 32 dr of range; pulses add their offset from the leaf centre.
-        double span = 0.0;
-        for (int i : plan->leaves) span = std::max(span, 32.0 * fabs(plan->nodes[i].dr));
-        const int wb = (int)ceil(span / fabs(data_dr)) + 48;
+        // A leaf tile spans rows_t dr of range; pulses add their offset from the leaf centre.
+        const int wb = (int)ceil(ffbp_leaf_tile_span(*plan) / fabs(data_dr)) + 48;
         const int ch = split_chunk_for(wb, plan->leaf_chunk, true);
         st = launch_split_ffbp_tables(in, nodes, plan->n_nodes, plan->max_dim, tables, s);
         if (st == SARBP_OK)

@@ -2,6 +2,8 @@
 // scene batch, which reuses plans built by sarbp_ffbp_plan_create).
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "common.cuh"
@@ -38,3 +40,14 @@ struct sarbp_ffbp_plan {
     unsigned long long queue_limit_ns = 5000000000ull;  // wait limit per merge item
     int withheld = -1;            // a node that never becomes ready (tests of the wait limit), or -1
 };
+
+// Range extent (m) of the tallest leaf tile of a split plan: the leaf kernel's range window per
+// pulse covers it plus the pulse's offset from the leaf centre.
+inline double ffbp_leaf_tile_span(const sarbp_ffbp_plan& p) {
+    double span = 0.0;
+    for (int i : p.leaves) {
+        const sarbp::PolarDesc& d = p.nodes[i];
+        span = std::max(span, (double)(sarbp::kSplitTilePixels >> d.tile_lc) * fabs(d.dr));
+    }
+    return span;
+}
