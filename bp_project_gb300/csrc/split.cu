@@ -1851,6 +1851,7 @@ struct PulseRec {
     float4 a;  // A_hi.x, A_hi.y, A_hi.z, frac(phase / 2pi)
     float4 b;  // A_lo.x, A_lo.y, A_lo.z, |pos - O|^2
     float4 c;  // (pos - O).x, .y, .z, weight
+    float4 d;  // the leaf's A quantum (a power of two), its inverse
 };
 
 __device__ __forceinline__ void leaf_pulses(double K, const double* __restrict__ pos, const double* __restrict__ weight,
@@ -1878,6 +1879,7 @@ __device__ __forceinline__ void leaf_pulses(double K, const double* __restrict__
         r.a.w = (float)(t - rint(t));
         r.b.w = (float)(ax * ax + ay * ay + az * az);
         r.c = make_float4((float)ax, (float)ay, (float)az, (float)weight[n]);
+        r.d = make_float4((float)scale, (float)inv_scale, 0.0f, 0.0f);
         recs[n] = r;
     }
 }
@@ -1895,28 +1897,163 @@ __global__ void ffbp_leaf_pulses_kernel(double K, const double* __restrict__ pos
 // a pixel at slant range r from O in unit direction e satisfies exactly
 //   d = |r e - a| = r - L + eps,  L = e . a,  eps = (|a|^2 - L^2) / (2 (r - L) + eps),
 // so the demodulated phase k (d - r) + phase_n is -K e . a + K eps + phase_n / 2pi
-// (turns): no large term, no per-tile FP64.  e comes from the row / column
-// tables as a quantized pair (2^-11), so A_hi . e_hi is exact.
+// (turns): no large term, no per-tile FP64.  On a polar grid e = (alpha s, alpha u, beta) with
+// alpha = g / r and beta = -oz / r per row and s = side sqrt(1 - u^2), u per column, so
+//   e . a = alpha C + beta a.z,       C = s a.x + u a.y,
+//   -K e . a = alpha D + beta A.z,    D = s A.x + u A.y   (A = -K a),
+// with C and D once per (pulse, tile column).  The phase's large part alpha_hi D_hi + beta_hi
+// A_hi.z is exact in FP32: alpha_hi and beta_hi are multiples of 2^-11 (11 bits), D_hi and
+// A_hi.z multiples of the leaf's A quantum below 2^10.5 quanta, so each product has at most 22
+// bits and their sum 23.  A thread's four pixels share the tile column and run as two pairs
+// of f32x2 lanes.
 struct LeafRec {
-    float4 a;  // A_hi.x, A_hi.y, A_hi.z, Phi
-    float4 b;  // A_lo.x, A_lo.y, A_lo.z, |a|^2
-    float4 c;  // a.x, a.y, a.z, window bias bits
-    float4 d;  // window offset bits, window count - 1 bits
+    float4 p0;  // (a.z, a.z), (-|a|^2, -|a|^2)
+    float4 p1;  // (A_hi.z, A_hi.z), (A_lo.z, A_lo.z)
+    float4 p2;  // (A.z, A.z), (Phi, Phi)
+    int4 w;     // window bias bits, window offset, window count - 1, unused
 };
 
-struct LPix {
-    float ex, ey, ez, exh, eyh, ezh, exl, eyl, ezl;
-    float r2, fm;
-    int rowoff;
-    float ar, ai;
+struct LeafCol {
+    float4 p0;  // (C, C), (D_hi, D_hi)
+    float4 p1;  // (D_lo, D_lo), (D, D)
+};
+
+constexpr int kLeafColStride = 32;  // LeafCol entries per pulse: the widest leaf tile
+
+__host__ __device__ constexpr size_t leaf_col_offset() { return (size_t)kMaxLeafChunk * sizeof(LeafRec); }
+__host__ __device__ constexpr size_t leaf_window_offset(int chunk) {
+    return leaf_col_offset() + (size_t)chunk * kLeafColStride * sizeof(LeafCol);
+}
+
+// Two pixels of one tile column (the lanes), rows (row0, row1).
+struct LPair {
+    float2 na, nb;  // -alpha, -beta
+    float2 ah, al;  // alpha = ah + al, ah a multiple of 2^-11
+    float2 bh, bl;  // beta = bh + bl
+    float2 r2, fm;  // 2 r, frac(Q) - 1/2 with Q = (r - range_start) / data_dr
+    float2 ar, ai;  // accumulated image, real and imaginary parts
+    int o0, o1;     // floor(Q) - I_first
 };
 
 constexpr float kUnitQ = 1.0f / 2048.0f;  // quantum of unit-vector components (11 bits)
 
-__device__ __forceinline__ void unit_pair(float p, float e, float& h, float& l, float& full) {
+__device__ __forceinline__ void unit_split(float p, float e, float& h, float& l, float& full) {
     h = rintf(p * 2048.0f) * kUnitQ;
     l = (p - h) + e;
     full = p + e;
+}
+
+// The row values of pixel row i (tables: (g/r, -oz/r) as float pairs, (2r, frac(Q) - 1/2, floor(Q))).
+__device__ __forceinline__ void leaf_row(const PolarDesc& g, const float4* __restrict__ tables, int i, int I_first,
+                                         float& na, float& nb, float& ah, float& al, float& bh, float& bl, float& r2,
+                                         float& fm, int& o) {
+    const float4 r1 = __ldg(tables + g.rows_off + 3 * (long long)i + 1);
+    const float4 rq = __ldg(tables + g.rows_off + 3 * (long long)i + 2);
+    float a, b;
+    unit_split(r1.x, r1.y, ah, al, a);
+    unit_split(r1.z, r1.w, bh, bl, b);
+    na = -a;
+    nb = -b;
+    r2 = rq.x;
+    fm = rq.y;
+    o = __float_as_int(rq.z) - I_first;
+}
+
+// One pixel's windowed sample (the reference's cubic, weight folded in) at bin index bits tq and
+// centred fraction s; with no fitting window the taps come straight from the pulse row.
+template <bool STAGED>
+__device__ __forceinline__ float2 leaf_sample(const float4* wrow, unsigned last, int bias, float tq,
+                                              float s, int o, const float2* drow, int I_first, int samples, float wt) {
+    float2 v;
+    if (STAGED) {
+        const unsigned j = min((unsigned)(__float_as_int(tq) + o - bias), last);
+        const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
+        const float2 sp = pair(s);
+        v = __ffma2_rn(make_float2(c23.z, c23.w), sp, make_float2(c23.x, c23.y));
+        v = __ffma2_rn(v, sp, make_float2(c01.z, c01.w));
+        v = __ffma2_rn(v, sp, make_float2(c01.x, c01.y));
+    } else {  // the pulse's window does not fit: gather its taps directly
+        const long long gb = (long long)(__float_as_int(tq) - kMagicBits) + o + I_first;
+        v = make_float2(0.0f, 0.0f);
+        if (gb >= 1 && gb <= (long long)samples - 3) {
+            float w[4];
+            lagrange_centred(s, w);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const float2 x = __ldg(drow + gb + b - 1);
+                v.x = fmaf(w[b], x.x, v.x);
+                v.y = fmaf(w[b], x.y, v.y);
+            }
+            v.x *= wt;
+            v.y *= wt;
+        }
+    }
+    return v;
+}
+
+// One pulse on one pixel pair: range, window sample, phase and the accumulation.
+template <bool STAGED>
+__device__ __forceinline__ void leaf_pair_pulse(LPair& q, const LeafRec& R, const LeafCol& Cc, const float4* wrow, unsigned last, int bias, const float2* drow,
+                                                int I_first, int samples, float wt, float2 nKf, float2 ninv_dr) {
+    const float2 magic = pair(kMagic), nmagic = pair(-kMagic), mone = pair(-1.0f);
+    const float2 az = make_float2(R.p0.x, R.p0.y), naa = make_float2(R.p0.z, R.p0.w);
+    const float2 C = make_float2(Cc.p0.x, Cc.p0.y);
+    const float2 nL = __ffma2_rn(q.na, C, __fmul2_rn(q.nb, az));  // -L
+    const float2 nq2 = __ffma2_rn(nL, nL, naa);                    // -(|a|^2 - L^2)
+    const float2 den = __ffma2_rn(pair(2.0f), nL, q.r2);           // 2 (r - L)
+    const float2 B = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+    const float2 ne0 = __fmul2_rn(nq2, B);
+    const float2 neps = __ffma2_rn(__fmul2_rn(ne0, ne0), B, ne0);  // -eps (second order: leaves are wide)
+    const float2 qp = __ffma2_rn(__ffma2_rn(nL, mone, neps), ninv_dr, q.fm);
+    const float2 tq = __fadd2_rn(qp, magic);
+    const float2 s = __ffma2_rn(__fadd2_rn(tq, nmagic), mone, qp);
+    // Phase (turns): the exact part, then the small terms.
+    const float2 tb = __ffma2_rn(q.ah, make_float2(Cc.p0.z, Cc.p0.w), __fmul2_rn(q.bh, make_float2(R.p1.x, R.p1.y)));
+    float2 sm = __ffma2_rn(nKf, neps, make_float2(R.p2.z, R.p2.w));
+    sm = __ffma2_rn(q.ah, make_float2(Cc.p1.x, Cc.p1.y), sm);
+    sm = __ffma2_rn(q.al, make_float2(Cc.p1.z, Cc.p1.w), sm);
+    sm = __ffma2_rn(q.bh, make_float2(R.p1.z, R.p1.w), sm);
+    sm = __ffma2_rn(q.bl, make_float2(R.p2.x, R.p2.y), sm);
+    // The reduced exact term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps (eps is second order in
+    // the pulse's offset from the leaf centre), so the angle stays within a few turns, which the
+    // hardware sin/cos reduce themselves.
+    const float2 rtb = __fadd2_rn(__fadd2_rn(tb, magic), nmagic);
+    const float2 ang = __fmul2_rn(__fadd2_rn(__ffma2_rn(rtb, mone, tb), sm), pair(kTwoPiF));
+    float sn0, cs0, sn1, cs1;
+    __sincosf(ang.x, &sn0, &cs0);
+    __sincosf(ang.y, &sn1, &cs1);
+    const float2 v0 = leaf_sample<STAGED>(wrow, last, bias, tq.x, s.x, q.o0, drow, I_first, samples, wt);
+    const float2 v1 = leaf_sample<STAGED>(wrow, last, bias, tq.y, s.y, q.o1, drow, I_first, samples, wt);
+    q.ar.x = fmaf(v0.x, cs0, q.ar.x);
+    q.ar.x = fmaf(-v0.y, sn0, q.ar.x);
+    q.ai.x = fmaf(v0.x, sn0, q.ai.x);
+    q.ai.x = fmaf(v0.y, cs0, q.ai.x);
+    q.ar.y = fmaf(v1.x, cs1, q.ar.y);
+    q.ar.y = fmaf(-v1.y, sn1, q.ar.y);
+    q.ai.y = fmaf(v1.x, sn1, q.ai.y);
+    q.ai.y = fmaf(v1.y, cs1, q.ai.y);
+}
+
+// C and D of one (pulse, tile column) from the pulse record and the column table (c, u pairs):
+// D in two-float, split on the leaf's A quantum.
+__device__ __forceinline__ LeafCol leaf_col(const PulseRec& pr, float4 cv, float side) {
+    const float sh = side * cv.x, sl = side * cv.y, uh = cv.z, ul = cv.w;
+    const float C = fmaf(sh, pr.c.x, uh * pr.c.y);
+    const float p1 = sh * pr.a.x, e1 = fmaf(sh, pr.a.x, -p1);
+    const float p2 = uh * pr.a.y, e2 = fmaf(uh, pr.a.y, -p2);
+    const float S = p1 + p2, bb = S - p1;
+    float rest = (p1 - (S - bb)) + (p2 - bb);
+    rest += e1 + e2;
+    rest = fmaf(sh, pr.b.x, rest);
+    rest = fmaf(sl, pr.a.x, rest);
+    rest = fmaf(uh, pr.b.y, rest);
+    rest = fmaf(ul, pr.a.y, rest);
+    const float Dh = rintf(S * pr.d.y) * pr.d.x;  // the A quantum is a power of two: exact
+    const float Dl = (S - Dh) + rest;             // S - Dh is exact (|S - Dh| <= quantum / 2)
+    LeafCol L;
+    L.p0 = make_float4(C, C, Dh, Dh);
+    L.p1 = make_float4(Dl, Dl, S + rest, S + rest);
+    return L;
 }
 
 // One leaf tile: the per-item body of the leaf kernels.  precs holds the pulse records of
@@ -1928,38 +2065,30 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
     const PolarDesc g = nodes[it.node];
     const int lc = g.tile_lc, cols_t = 1 << lc, rows_t = kSplitTilePixels >> lc;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const float side = (float)g.side;
+    const int col = tid & (cols_t - 1);
     const int ifirst = min(g.win_r0 + it.tile_r, g.nr - 1);
     const int ilast = min(g.win_r0 + it.tile_r + rows_t - 1, g.nr - 1);
     const float4 rfirst = __ldg(tables + g.rows_off + 3 * (long long)ifirst + 2);
     const int I_first = __float_as_int(rfirst.z);
     const int I_span = __float_as_int(__ldg(tables + g.rows_off + 3 * (long long)ilast + 2).z) - I_first;
     const float r_min = 0.5f * rfirst.x;
-    LPix px[kPX];
+    // Pixel k of this thread is row (tid >> lc) + k (256 >> lc) of its column; pairs (0, 1), (2, 3).
+    LPair px[2];
 #pragma unroll
-    for (int k = 0; k < kPX; ++k) {
-        const int p = tid + kThreads * k;
-        const int i = min(g.win_r0 + it.tile_r + (p >> lc), g.nr - 1);
-        const int j = min(g.win_u0 + it.tile_u + (p & (cols_t - 1)), g.nu - 1);
-        const float4 r1 = __ldg(tables + g.rows_off + 3 * (long long)i + 1);
-        const float4 r2 = __ldg(tables + g.rows_off + 3 * (long long)i + 2);
-        const float4 cv = __ldg(tables + g.cols_off + j);
-        LPix& q = px[k];
-        float pp, ee;
-        two_prod(r1.x, r1.y, cv.x, cv.y, pp, ee);
-        unit_pair(side * pp, side * ee, q.exh, q.exl, q.ex);
-        two_prod(r1.x, r1.y, cv.z, cv.w, pp, ee);
-        unit_pair(pp, ee, q.eyh, q.eyl, q.ey);
-        unit_pair(r1.z, r1.w, q.ezh, q.ezl, q.ez);
-        q.r2 = r2.x;
-        q.fm = r2.y;
-        q.rowoff = __float_as_int(r2.z) - I_first;
-        q.ar = q.ai = 0.0f;
+    for (int h = 0; h < 2; ++h) {
+        LPair& q = px[h];
+        const int i0 = min(g.win_r0 + it.tile_r + (tid >> lc) + (kThreads >> lc) * (2 * h), g.nr - 1);
+        const int i1 = min(g.win_r0 + it.tile_r + (tid >> lc) + (kThreads >> lc) * (2 * h + 1), g.nr - 1);
+        leaf_row(g, tables, i0, I_first, q.na.x, q.nb.x, q.ah.x, q.al.x, q.bh.x, q.bl.x, q.r2.x, q.fm.x, q.o0);
+        leaf_row(g, tables, i1, I_first, q.na.y, q.nb.y, q.ah.y, q.al.y, q.bh.y, q.bl.y, q.r2.y, q.fm.y, q.o1);
+        q.ar = q.ai = make_float2(0.0f, 0.0f);
     }
     LeafRec* rec = reinterpret_cast<LeafRec*>(smem);
-    float4* win = reinterpret_cast<float4*>(smem + (size_t)kMaxLeafChunk * sizeof(LeafRec));
+    LeafCol* cols = reinterpret_cast<LeafCol*>(smem + leaf_col_offset());
+    float4* win = reinterpret_cast<float4*>(smem + leaf_window_offset(P.chunk));
     const PulseInputs& in = P.in;
-    const float inv_dr = P.inv_drf, Kf = P.Kf;
+    const float2 nKf = pair(-P.Kf), ninv_dr = pair(-P.inv_drf);
+    const float side = (float)g.side;
     for (int c0 = g.a; c0 < g.b;) {
         const int want = min(P.chunk, g.b - c0);
         __syncthreads();
@@ -1969,17 +2098,18 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
                 const PulseRec pr = precs[c0 + lane];
                 const float amag = sqrtf(pr.b.w);
                 const float eps_max = pr.b.w / (2.0f * fmaxf(r_min - amag, 1.0f));
-                const float hw = (amag + eps_max) * fabsf(inv_dr) + 1e-3f;
+                const float hw = (amag + eps_max) * fabsf(P.inv_drf) + 1e-3f;
                 const int bo = (int)floorf(-0.5f - hw), top = (int)ceilf(0.5f + hw);
                 const long long cnt = (long long)I_span + top - bo + 1;
                 count = cnt <= P.cap ? (int)cnt : P.cap + 1;
                 s_base[lane] = I_first + bo;
                 s_wt[lane] = pr.c.w;
                 LeafRec r;
-                r.a = pr.a;
-                r.b = pr.b;
-                r.c = make_float4(pr.c.x, pr.c.y, pr.c.z, __int_as_float(kMagicBits + bo));
-                r.d = make_float4(0.0f, __int_as_float(count - 1), 0.0f, 0.0f);
+                r.p0 = make_float4(pr.c.z, pr.c.z, -pr.b.w, -pr.b.w);
+                r.p1 = make_float4(pr.a.z, pr.a.z, pr.b.z, pr.b.z);
+                const float Az = pr.a.z + pr.b.z;
+                r.p2 = make_float4(Az, Az, pr.a.w, pr.a.w);
+                r.w = make_int4(kMagicBits + bo, 0, count - 1, 0);
                 rec[lane] = r;
             }
             int inc = count;
@@ -1989,16 +2119,21 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
                 if (lane >= o) inc += v;
             }
             const unsigned fits = __ballot_sync(0xffffffffu, lane < want && inc <= P.cap);
-            if (lane < want) rec[lane].d.x = __int_as_float(inc - count);
+            if (lane < want) rec[lane].w.y = inc - count;
             if (lane == 0) s_nfit = __popc(fits);
         }
         __syncthreads();
         const int nfit = s_nfit;
         const int chn = nfit > 0 ? nfit : 1;
+        for (int e = tid; e < (chn << lc); e += kThreads) {  // C, D per (pulse, column)
+            const int nl = e >> lc, cc = e & (cols_t - 1);
+            const float4 cv = __ldg(tables + g.cols_off + min(g.win_u0 + it.tile_u + cc, g.nu - 1));
+            cols[nl * kLeafColStride + cc] = leaf_col(precs[c0 + nl], cv, side);
+        }
         if (nfit > 0) {
             for (int nl = warp; nl < nfit; nl += kThreads / 32) {
-                const int off = __float_as_int(rec[nl].d.x);
-                const int cnt = __float_as_int(rec[nl].d.y) + 1;
+                const int off = rec[nl].w.y;
+                const int cnt = rec[nl].w.z + 1;
                 const long long b0 = s_base[nl];
                 const float a = s_wt[nl];
                 const float2* row = in.data + (size_t)(c0 + nl) * in.samples;
@@ -2012,76 +2147,39 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
                     win[2 * (off + jj) + 1] = c23;
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
+        if (nfit > 0) {
 #pragma unroll 1
-        for (int nl = 0; nl < chn; ++nl) {
-            const float4 ra = rec[nl].a, rb = rec[nl].b, rc = rec[nl].c, rd = rec[nl].d;
-            const int bias = __float_as_int(rc.w);
-            const unsigned last = (unsigned)__float_as_int(rd.y);
-            const float4* wrow = win + 2 * __float_as_int(rd.x);
-            const float2* drow = in.data + (size_t)(c0 + nl) * in.samples;
+            for (int nl = 0; nl < nfit; ++nl) {
+                const LeafRec R = rec[nl];
+                const LeafCol Cc = cols[nl * kLeafColStride + col];
+                const float4* wrow = win + 2 * R.w.y;
 #pragma unroll
-            for (int k = 0; k < kPX; ++k) {
-                LPix& q = px[k];
-                const float L = fmaf(rc.x, q.ex, fmaf(rc.y, q.ey, rc.z * q.ez));
-                const float q2 = fmaf(-L, L, rb.w);
-                const float B = rcp_approx(fmaf(-2.0f, L, q.r2));
-                const float e0 = q2 * B;
-                const float eps = fmaf(-e0 * e0, B, e0);  // second order: leaves can be tens of metres wide
-                const float qp = fmaf(eps - L, inv_dr, q.fm);
-                const float tq = qp + kMagic;
-                const float s = qp - (tq - kMagic);
-                float vr, vi;
-                if (nfit > 0) {
-                    const unsigned j = min((unsigned)(__float_as_int(tq) + q.rowoff - bias), last);
-                    const float4 c01 = wrow[2 * j], c23 = wrow[2 * j + 1];
-                    vr = fmaf(fmaf(fmaf(c23.z, s, c23.x), s, c01.z), s, c01.x);
-                    vi = fmaf(fmaf(fmaf(c23.w, s, c23.y), s, c01.w), s, c01.y);
-                } else {  // the pulse's window does not fit: gather its taps directly
-                    const long long gb = (long long)(__float_as_int(tq) - kMagicBits) + q.rowoff + I_first;
-                    vr = vi = 0.0f;
-                    if (gb >= 1 && gb <= (long long)in.samples - 3) {
-                        float w[4];
-                        lagrange_centred(s, w);
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) {
-                            const float2 v = __ldg(drow + gb + b - 1);
-                            vr = fmaf(w[b], v.x, vr);
-                            vi = fmaf(w[b], v.y, vi);
-                        }
-                        vr *= s_wt[nl];
-                        vi *= s_wt[nl];
-                    }
-                }
-                float tb = fmaf(ra.x, q.exh, fmaf(ra.y, q.eyh, ra.z * q.ezh));  // exact
-                float sm = fmaf(Kf, eps, ra.w);
-                sm = fmaf(ra.x, q.exl, sm);
-                sm = fmaf(ra.y, q.eyl, sm);
-                sm = fmaf(ra.z, q.ezl, sm);
-                sm = fmaf(rb.x, q.ex, sm);
-                sm = fmaf(rb.y, q.ey, sm);
-                sm = fmaf(rb.z, q.ez, sm);
-                // The reduced exact term is in [-1/2, 1/2] turn and |sm| <= 1 + K eps (eps is second
-                // order in the pulse's offset from the leaf centre), so the angle stays within a few
-                // turns, which the hardware sin/cos reduce themselves.
-                const float ang = ((tb - round_magic(tb)) + sm) * kTwoPiF;
-                float sn, cs;
-                __sincosf(ang, &sn, &cs);
-                q.ar = fmaf(vr, cs, q.ar);
-                q.ar = fmaf(-vi, sn, q.ar);
-                q.ai = fmaf(vr, sn, q.ai);
-                q.ai = fmaf(vi, cs, q.ai);
+                for (int h = 0; h < 2; ++h)
+                    leaf_pair_pulse<true>(px[h], R, Cc, wrow, (unsigned)R.w.z, R.w.x, nullptr, I_first, in.samples, 0.0f,
+                                          nKf, ninv_dr);
             }
+        } else {  // one pulse whose window does not fit: its taps come straight from the pulse row
+            const LeafRec R = rec[0];
+            const LeafCol Cc = cols[col];
+            const float2* drow = in.data + (size_t)c0 * in.samples;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                leaf_pair_pulse<false>(px[h], R, Cc, nullptr, 0u, 0, drow, I_first, in.samples, s_wt[0], nKf, ninv_dr);
         }
         c0 += chn;
     }
     float2* dst = g.dst ? g.dst : (it.node == root ? root_out : arena + g.out_offset);
+    const int wu = it.tile_u + col;
 #pragma unroll
-    for (int k = 0; k < kPX; ++k) {
-        const int p = tid + kThreads * k;
-        const int wr = it.tile_r + (p >> lc), wu = it.tile_u + (p & (cols_t - 1));
-        if (wr < g.win_nr && wu < g.win_nu) dst[(long long)wr * g.out_stride + wu] = make_float2(px[k].ar, px[k].ai);
+    for (int h = 0; h < 2; ++h) {
+        const int wr0 = it.tile_r + (tid >> lc) + (kThreads >> lc) * (2 * h);
+        const int wr1 = wr0 + (kThreads >> lc);
+        if (wu < g.win_nu) {
+            if (wr0 < g.win_nr) dst[(long long)wr0 * g.out_stride + wu] = make_float2(px[h].ar.x, px[h].ai.x);
+            if (wr1 < g.win_nr) dst[(long long)wr1 * g.out_stride + wu] = make_float2(px[h].ar.y, px[h].ai.y);
+        }
     }
 }
 
@@ -2671,6 +2769,12 @@ int capacity_for(int chunk, int window_bins, int budget_bytes = kWindowBudget) {
     return (int)(cap > budget ? budget : cap);
 }
 
+// Leaf window entries: the windows share the CTA's shared memory with the chunk's pulse and
+// (pulse, column) records, within the same per-CTA total as the direct kernels' windows.
+int leaf_capacity(int chunk, int window_bins) {
+    return capacity_for(chunk, window_bins, kWindowBudget - (int)leaf_window_offset(chunk));
+}
+
 }  // namespace
 
 int split_window_bins(double radius, double data_dr) {
@@ -2843,8 +2947,8 @@ int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, cons
                              int chunk, int window_bins, const float4* tables, const void* precs, float2* arena,
                              float2* root_out, int root, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
-    SplitParams P = make_params(in, chunk, capacity_for(chunk, window_bins), 1);
-    const size_t smem = (size_t)kMaxLeafChunk * sizeof(LeafRec) + (size_t)P.cap * 32;
+    SplitParams P = make_params(in, chunk, leaf_capacity(chunk, window_bins), 1);
+    const size_t smem = leaf_window_offset(chunk) + (size_t)P.cap * 32;
     if (int st = prepare(split_leaf_kernel, smem)) return st;
     split_leaf_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const PulseRec*>(precs),
                                                      arena, root_out, root);
@@ -3083,7 +3187,7 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     BatchScene b{};
     b.P = make_params(d.in, d.chunk,
                       d.kind == 0 ? capacity_for(d.chunk, d.window_bins, kLatticeWindowBudget)
-                                  : capacity_for(d.chunk, d.window_bins),
+                                  : leaf_capacity(d.chunk, d.window_bins),
                       1);
     b.P.out = d.out;
     b.lat = d.lat;
@@ -3091,7 +3195,7 @@ size_t split_batch_pack_scene(const BatchSceneDesc& d, void* dst) {
     b.lc = d.lc;
     b.prec_offset = d.prec_offset;
     memcpy(dst, &b, sizeof(b));
-    return (d.kind == 0 ? window_offset() + raw_bytes_for(b.P.cap, kMaxChunk) : (size_t)kMaxLeafChunk * sizeof(LeafRec)) +
+    return (d.kind == 0 ? window_offset() + raw_bytes_for(b.P.cap, kMaxChunk) : leaf_window_offset(d.chunk)) +
            (size_t)b.P.cap * 32;
 }
 
