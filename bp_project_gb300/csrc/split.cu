@@ -42,6 +42,9 @@ namespace {
 
 constexpr int kThreads = kSplitThreads;
 constexpr int kPX = 4;
+// Threads of the single-scene merge kernel: four column pairs of parent pixels per thread (more
+// gathers in flight per warp than two pairs at 256 threads).
+constexpr int kMergeThreads = 128;
 constexpr int kMaxRows = kSplitTilePixels >> 2;  // tile_lc >= 2
 constexpr int kMaxCols = 32;                     // tile_lc <= 5
 constexpr int kMaxChunk = 64;      // pulses per chunk of the direct kernels: two warps compute the records
@@ -420,6 +423,7 @@ __device__ __forceinline__ void tab_quantum(const PolarDesc& g, int lc, int tile
 // Polar merge-tile set-up from per-node tables of float pairs (FFBP): FP32 two-float arithmetic
 // only, one barrier.  The offsets are quantized on the tile's quantum (q, iq) from its child
 // record, so each table entry is final when it is written.
+template <int THREADS>
 __device__ void setup_polar_tab(const Job& J, TabF& T, const float4* __restrict__ tables, float q, float iq) {
     const PolarDesc& g = J.g;
     const int tid = threadIdx.x;
@@ -427,18 +431,24 @@ __device__ void setup_polar_tab(const Job& J, TabF& T, const float4* __restrict_
     float4 r0v, c0v;
     int j0;
     tab_centre(g, J.lc, J.tile_r, J.tile_u, tables, r0v, c0v, j0);
-    if (tid < rows_t) {
-        TabRow R = tab_row(g, tables, r0v, c0v, min(g.win_r0 + J.tile_r + tid, g.nr - 1));
+    // rows_t <= 256: one row per thread, or a loop when the block is narrower.
+    const auto row = [&](int t) {
+        TabRow R = tab_row(g, tables, r0v, c0v, min(g.win_r0 + J.tile_r + t, g.nr - 1));
         quantize_pair(R.rxh, R.rxl, q, iq);
         quantize_pair(R.ryh, R.ryl, q, iq);
-        T.rxh[tid] = R.rxh;
-        T.rxl[tid] = R.rxl;
-        T.ryh[tid] = R.ryh;
-        T.ryl[tid] = R.ryl;
-        T.dg[tid] = R.dg;
-        T.psi[tid] = R.psi;
+        T.rxh[t] = R.rxh;
+        T.rxl[t] = R.rxl;
+        T.ryh[t] = R.ryh;
+        T.ryl[t] = R.ryl;
+        T.dg[t] = R.dg;
+        T.psi[t] = R.psi;
+    };
+    if (THREADS >= kMaxRows) {
+        if (tid < rows_t) row(tid);
+    } else {
+        for (int t = tid; t < rows_t; t += THREADS) row(t);
     }
-    if (tid < cols_t) {
+    if (tid < cols_t) {  // cols_t <= 32
         TabCol C = tab_col(g, tables, r0v, c0v, min(g.win_u0 + J.tile_u + tid, g.nu - 1), j0);
         quantize_pair(C.cxh, C.cxl, q, iq);
         quantize_pair(C.cyh, C.cyl, q, iq);
@@ -2554,10 +2564,10 @@ __device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const V
 
 // One merge tile: both children regridded onto the parent tile, each rounded to complex64,
 // then added (the reference's rounding points).  crec points at the tile's two child records.
-// Thread t forms the column pairs (rows 2 m and 2 m + 1 of column t mod cols) for
-// m = t / cols and m + 256 / cols; its offsets come back from the shared tables per pair, which
+// Thread t of THREADS forms the column pairs (rows 2 m and 2 m + 1 of column t mod cols) for
+// m = t / cols + i THREADS / cols; its offsets come back from the shared tables per pair, which
 // keeps the live state small.
-template <bool COHERENT = false>
+template <bool COHERENT = false, int THREADS = kThreads>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
                                            ChildDup* C, float2* __restrict__ arena, float2* root_out, int root,
@@ -2570,13 +2580,14 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     if (threadIdx.x < 2) child_dup_store(crec[threadIdx.x], C[threadIdx.x]);
     const float4 d0 = __ldg(&crec[0].d);  // (G, frac(Qu) - 1/2, tile quantum, its inverse)
     TabF& T = *reinterpret_cast<TabF*>(smem);
-    setup_polar_tab(J, T, tables, d0.z, d0.w);
+    setup_polar_tab<THREADS>(J, T, tables, d0.z, d0.w);
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
     const int col = threadIdx.x & ((1 << J.lc) - 1), wu = J.tile_u + col;
-    float2 m[kPX];
+    constexpr int kPairs = kSplitTilePixels / (2 * THREADS);  // column pairs per thread
+    float2 m[2 * kPairs];
 #pragma unroll
-    for (int k = 0; k < kPX / 2; ++k) {
-        const int row = 2 * ((threadIdx.x >> J.lc) + (kThreads >> J.lc) * k);
+    for (int k = 0; k < kPairs; ++k) {
+        const int row = 2 * ((threadIdx.x >> J.lc) + (THREADS >> J.lc) * k);
         const VPix v = tab_vpair(T, row, col);
         float2 a0, b0, a1, b1;
         child_vpair<COHERENT>(Kf, C[0], v, a0, b0);
@@ -2597,8 +2608,8 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     }
     if (COHERENT) {
 #pragma unroll
-        for (int k = 0; k < kPX / 2; ++k) {
-            const int wr = J.tile_r + 2 * ((threadIdx.x >> J.lc) + (kThreads >> J.lc) * k);
+        for (int k = 0; k < kPairs; ++k) {
+            const int wr = J.tile_r + 2 * ((threadIdx.x >> J.lc) + (THREADS >> J.lc) * k);
             if (wu < J.g.win_nu) {
                 if (wr < J.g.win_nr) dst[(long long)wr * J.g.out_stride + wu] = m[2 * k];
                 if (wr + 1 < J.g.win_nr) dst[(long long)(wr + 1) * J.g.out_stride + wu] = m[2 * k + 1];
@@ -2607,7 +2618,7 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 5) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
+__global__ void __launch_bounds__(kMergeThreads, 8) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items,
                                                                   const float4* __restrict__ tables,
                                                                   const ChildRec* __restrict__ crecs,
@@ -2615,7 +2626,8 @@ __global__ void __launch_bounds__(kThreads, 5) split_merge_kernel(SplitParams P,
                                                                   int root) {
     extern __shared__ __align__(16) char smem[];
     __shared__ ChildDup C[2];
-    merge_tile(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena, root_out, root, smem);
+    merge_tile<false, kMergeThreads>(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena,
+                                     root_out, root, smem);
 }
 
 // All merge levels in one persistent launch.  Items are in height order; a CTA claims the next
@@ -2966,7 +2978,7 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
     SplitParams P = make_params(none, 1, 4, 1);
     const size_t smem = merge_smem();
     if (int st = prepare(split_merge_kernel, smem)) return st;
-    split_merge_kernel<<<nitems, kThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs),
+    split_merge_kernel<<<nitems, kMergeThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs),
                                                       arena, root_out, root);
     note_launches(1);
     return check_launch("split_ffbp_merges");
@@ -3135,7 +3147,7 @@ __global__ void __launch_bounds__(kThreads, 3) batch_leaf_kernel(const BatchScen
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 5) batch_merge_kernel(const BatchScene* __restrict__ scenes,
+__global__ void __launch_bounds__(kMergeThreads, 8) batch_merge_kernel(const BatchScene* __restrict__ scenes,
                                                                   const PolarDesc* __restrict__ nodes,
                                                                   const TileItem* __restrict__ items, int nitems,
                                                                   const float4* __restrict__ tables,
@@ -3149,7 +3161,8 @@ __global__ void __launch_bounds__(kThreads, 5) batch_merge_kernel(const BatchSce
         const int idx = next_item(counter, s_item);
         if (idx >= nitems) return;
         const TileItem it = items[idx];
-        merge_tile(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena, nullptr, -1, smem);
+        merge_tile<false, kMergeThreads>(scenes[it.pad].P.Kf, nodes, it, tables, crecs + 2 * (long long)idx, C, arena,
+                                         nullptr, -1, smem);
         trace_item(trace, it.pad);
     }
 }
@@ -3209,7 +3222,7 @@ int split_batch_occupancy(size_t direct_smem, size_t leaf_smem, int* direct_per_
     if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(leaf_per_sm, batch_leaf_kernel, kThreads, leaf_smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_per_sm, batch_merge_kernel, kThreads, merge_smem());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(merge_per_sm, batch_merge_kernel, kMergeThreads, merge_smem());
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "occupancy query: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
@@ -3271,7 +3284,7 @@ int launch_split_batch_merges(const void* scenes, const PolarDesc* nodes, const 
                               unsigned long long* trace, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     if (int st = prepare(batch_merge_kernel, merge_smem())) return st;
-    batch_merge_kernel<<<blocks, kThreads, merge_smem(), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
+    batch_merge_kernel<<<blocks, kMergeThreads, merge_smem(), s>>>(reinterpret_cast<const BatchScene*>(scenes), nodes,
                                                               items, nitems, tables,
                                                               reinterpret_cast<const ChildRec*>(crecs), arena,
                                                               counter, trace);
