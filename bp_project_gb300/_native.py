@@ -130,6 +130,8 @@ SIGNATURES = {
     "sarbp_wait_timeouts": ([ctypes.POINTER(_I)], _I),
     "sarbp_ffbp_set_node_image": ([_P, _I, _P, _P], _I),
     "sarbp_ffbp_set_merge_queue": ([_P, _I], _I),
+    "sarbp_ffbp_set_staging": ([_P, _I], _I),
+    "sarbp_ffbp_staging": ([_P, _P], _I),
     "sarbp_ffbp_set_wait_limit": ([_P, _D, _I], _I),
     "sarbp_ffbp_status": ([_P, ctypes.POINTER(_I)], _I),
 }

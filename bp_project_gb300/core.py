@@ -295,9 +295,11 @@ class FFBPProgram:
     (origin, r0, dr, nr, u0, du, nu, side, a, b, left/right children).  The
     root's crop window is fused into the last merge, which writes the output
     directly.  The workspace (node images + device tables) is allocated once.
+    In split mode the merge tiles stage their children's footprints in shared memory by TMA
+    (``staging=False``: they gather from the child images; the image is the same).
     """
 
-    def __init__(self, nodes, crop_r, crop_u, mode=DEFAULT_MODE, device="cuda", merge_queue=False):
+    def __init__(self, nodes, crop_r, crop_u, mode=DEFAULT_MODE, device="cuda", merge_queue=False, staging=True):
         self.mode = mode
         arr = node_array(nodes)
         self.crop = (int(crop_r[0]), int(crop_u[0]), int(crop_r[1] - crop_r[0]), int(crop_u[1] - crop_u[0]))
@@ -309,12 +311,17 @@ class FFBPProgram:
         if merge_queue:
             # all merge levels as one dependency-counting launch instead of one launch per tree height
             nat.check(lib.sarbp_ffbp_set_merge_queue(handle, 1), "ffbp_set_merge_queue")
+        if not staging:
+            nat.check(lib.sarbp_ffbp_set_staging(handle, 0), "ffbp_set_staging")
         self.workspace_bytes = int(lib.sarbp_ffbp_workspace_bytes(handle))
         self.launch_count = int(lib.sarbp_ffbp_launch_count(handle))
         self.workspace = torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8, device=device)
         nat.check(lib.sarbp_ffbp_bind(handle, _ptr(self.workspace), self.workspace.numel(), stream_handle()),
                   "ffbp_bind")
         self.shape = (self.crop[2], self.crop[3])
+        staged = ctypes.c_int(0)
+        nat.check(lib.sarbp_ffbp_staging(handle, ctypes.byref(staged)), "ffbp_staging")
+        self.staged = bool(staged.value)
 
     def execute(self, data, pos, weight, phase, range_start, data_dr, k, out=None):
         p, s = check_pulses(data, pos, weight, phase)

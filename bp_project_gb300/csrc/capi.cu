@@ -9,6 +9,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "common.cuh"
 #include "plan.cuh"
 
@@ -135,6 +138,125 @@ constexpr double kPointRadius = 24.0;
 // Split-mode merge tiles may be up to this factor wider (in radius) than the squarest shape:
 // a warp's pixels then span fewer rows, and its stencil gathers fewer sectors.
 constexpr double kMergeTileSlack = 1.5;
+
+// Child-image coordinates (range bin, angle bin; fractional) of pixel (i, j) of the parent grid
+// p, in FP64: the child polar grid's r and u = dy / g of the pixel's ground point (the
+// quantities the merge kernel computes in FP32 per pixel).
+void child_bins(const PolarDesc& p, const PolarDesc& c, int i, int j, double& qr, double& qu) {
+    const double r = p.r0 + i * p.dr, u = p.u0 + j * p.du;
+    const double g = sqrt(fmax(r * r - p.oz * p.oz, 0.0));
+    const double x = p.ox + p.side * g * sqrt(fmax(1.0 - u * u, 0.0)), y = p.oy + g * u;
+    const double vx = x - c.ox, vy = y - c.oy;
+    const double gc = sqrt(vx * vx + vy * vy), rr = sqrt(gc * gc + c.oz * c.oz);
+    qr = (rr - c.r0) / c.dr;
+    qu = (vy / gc - c.u0) / c.du;
+}
+
+// Footprint boxes of split-mode merges (PolarDesc::box_*, PolarDesc of each child): the child
+// stencil rows and columns that a parent tile reads, relative to the stencil bin of the tile's
+// centre pixel, over the corners and edge midpoints of up to 16 x 16 tiles of each parent
+// (evenly spaced, the first and last included), plus one bin of margin on every side.  The
+// mapping is smooth over a tile, so the sampled extremes bound the rest up to that margin; a
+// warp whose stencils fall outside the staged box reads the child image instead.  A box over
+// 256 rows or columns (the TMA's limit) or kMaxChildBox bytes is not staged.  Also sets
+// merge_box_bytes per height.
+void child_footprints(sarbp_ffbp_plan& p) {
+    p.merge_box_bytes.assign(p.max_height + 1, 0);
+    for (int n = 0; n < p.n_nodes; ++n) {
+        const PolarDesc& d = p.nodes[n];
+        if (d.left < 0) continue;
+        const int cols_t = 1 << d.tile_lc, rows_t = kSplitTilePixels >> d.tile_lc;
+        const int ntr = (d.win_nr + rows_t - 1) / rows_t, ntu = (d.win_nu + cols_t - 1) / cols_t;
+        const int sr = std::min(ntr, 16), su = std::min(ntu, 16);
+        size_t bytes = 0;
+        for (int ch : {d.left, d.right}) {
+            PolarDesc& c = p.nodes[ch];
+            double lo_r = 0, hi_r = 0, lo_u = 0, hi_u = 0;
+            bool finite = true;
+            for (int a = 0; a < sr; ++a) {
+                const int tr = sr > 1 ? (int)((long long)a * (ntr - 1) / (sr - 1)) : 0;
+                const int r_first = d.win_r0 + tr * rows_t, r_last = std::min(r_first + rows_t - 1, d.nr - 1);
+                const int i0 = std::min(r_first + (rows_t >> 1), d.nr - 1);
+                for (int b = 0; b < su; ++b) {
+                    const int tu = su > 1 ? (int)((long long)b * (ntu - 1) / (su - 1)) : 0;
+                    const int u_first = d.win_u0 + tu * cols_t, u_last = std::min(u_first + cols_t - 1, d.nu - 1);
+                    const int j0 = std::min(u_first + (cols_t >> 1), d.nu - 1);
+                    double qr, qu;
+                    child_bins(d, c, i0, j0, qr, qu);
+                    const double ir = floor(qr), iu = floor(qu);
+                    const int is[3] = {r_first, (r_first + r_last) / 2, r_last};
+                    const int js[3] = {u_first, (u_first + u_last) / 2, u_last};
+                    for (int i : is)
+                        for (int j : js) {
+                            child_bins(d, c, i, j, qr, qu);
+                            if (!std::isfinite(qr) || !std::isfinite(qu) || !std::isfinite(ir) || !std::isfinite(iu)) {
+                                finite = false;
+                                continue;
+                            }
+                            const double fr = floor(qr), fu = floor(qu);
+                            lo_r = fmax(lo_r, ir - (fr - 1.0));
+                            hi_r = fmax(hi_r, fr + 2.0 - ir);
+                            lo_u = fmax(lo_u, iu - (fu - 1.0));
+                            hi_u = fmax(hi_u, fu + 2.0 - iu);
+                        }
+                }
+            }
+            c.box_w = 0;
+            if (!finite || lo_r + hi_r > 250.0 || lo_u + hi_u > 250.0) continue;
+            const int br = (int)lo_r + 1, bu = (int)lo_u + 1;
+            const int bh = std::max(br + (int)hi_r + 1 + 1, 8);       // the kernel's box tests need >= 5 x 4
+            int bw = std::max(bu + (int)hi_u + 1 + 2, 8);  // +1: the first column is rounded down to an even one
+            bw += bw & 1;
+            if (bh > 256 || bw > 256 || split_box_bytes(bh, bw) > kMaxChildBox) continue;
+            c.box_r = br;
+            c.box_u = bu;
+            c.box_h = bh;
+            c.box_w = bw;
+            bytes += split_box_bytes(bh, bw);
+        }
+        const int h = p.height[n];
+        p.merge_box_bytes[h] = std::max(p.merge_box_bytes[h], bytes);
+    }
+}
+
+// The driver's tensor-map encoder, through the runtime's entry-point query (no link against
+// the driver library); NULL where the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// One 2-D tensor map per child image with a footprint box (8-byte elements, nu x nr, row pitch
+// out_stride elements, box box_w x box_h, zero fill outside the image); the others stay zero.
+bool encode_child_maps(const sarbp_ffbp_plan& p, float2* arena, std::vector<CUtensorMap>& maps) {
+    static_assert(sizeof(CUtensorMap) == kTensorMapBytes, "tensor map size");
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return false;
+    maps.assign(p.n_nodes, CUtensorMap{});
+    for (int n = 0; n < p.n_nodes; ++n) {
+        const PolarDesc& c = p.nodes[n];
+        if (n == 0 || c.box_w <= 0) continue;
+        const cuuint64_t dims[2] = {(cuuint64_t)c.nu, (cuuint64_t)c.nr};
+        const cuuint64_t pitch[1] = {(cuuint64_t)c.out_stride * sizeof(float2)};
+        const cuuint32_t box[2] = {(cuuint32_t)c.box_w, (cuuint32_t)c.box_h};
+        const cuuint32_t unit[2] = {1, 1};
+        if (encode(&maps[n], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, arena + c.out_offset, dims, pitch, box, unit,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
+}
 
 }  // namespace
 
@@ -514,9 +636,11 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
             d.out_offset = 0;
             d.out_stride = crop_nu;
         } else {
+            // Split mode: rows of an even number of elements, so that every row starts on a
+            // 16-byte boundary (the TMA copies of the merge tiles' footprints need that).
             d.out_offset = (long long)(arena / sizeof(float2));
-            d.out_stride = d.nu;
-            arena += align_up((size_t)d.nr * d.nu * sizeof(float2));
+            d.out_stride = mode == SARBP_SPLIT ? d.nu + (d.nu & 1) : d.nu;
+            arena += align_up((size_t)d.nr * d.out_stride * sizeof(float2));
         }
         d.rows_off = p->table_entries;
         d.cols_off = p->table_entries + 3LL * d.nr;
@@ -602,11 +726,16 @@ int sarbp_ffbp_plan_create(const sarbp_ffbp_node* nodes, int n_nodes, int crop_r
         // [next, status] then live remaining, live pending, parent, initial remaining, initial pending
         p->queue_bytes = align_up(sizeof(int) * (2 + 5 * (size_t)n_nodes));
     }
+    if (mode == SARBP_SPLIT) {
+        child_footprints(*p);
+        p->tmap_bytes = align_up(kTensorMapBytes * (size_t)n_nodes);
+    }
     p->table_offset = p->node_bytes + p->work_bytes + p->leaf_list_bytes;
     p->prec_offset = p->table_offset + p->table_bytes;
     p->crec_offset = p->prec_offset + p->prec_bytes;
     p->queue_offset = p->crec_offset + p->crec_bytes;
-    p->arena_offset = p->queue_offset + p->queue_bytes;
+    p->tmap_offset = p->queue_offset + p->queue_bytes;
+    p->arena_offset = p->tmap_offset + p->tmap_bytes;
     p->arena_bytes = arena;
     p->total_bytes = p->arena_offset + arena;
     p->launches = p->max_height + 1 + (mode == SARBP_SPLIT ? 3 : 0);
@@ -653,7 +782,18 @@ int sarbp_ffbp_bind(sarbp_ffbp_plan* plan, void* workspace, size_t workspace_byt
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // `pending` is a host temporary
         }
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // Tensor maps of the child images (merge tiles stage their footprints by TMA); without the
+    // driver's encoder the merges gather from the child images instead (the same image).
+    std::vector<CUtensorMap> maps;
+    plan->staged = false;
+    if (e == cudaSuccess && plan->mode == SARBP_SPLIT && plan->staging && plan->tmap_bytes) {
+        float2* arena = reinterpret_cast<float2*>(base + plan->arena_offset);
+        plan->staged = encode_child_maps(*plan, arena, maps);
+        if (plan->staged)
+            e = cudaMemcpyAsync(base + plan->tmap_offset, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // also keeps `maps` alive until its copy is done
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "FFBP bind: %s", cudaGetErrorString(e));
     plan->bound = workspace;
     plan->bound_bytes = workspace_bytes;
@@ -669,8 +809,9 @@ int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float
     if (!(d.left < 0 && d.a < 0)) return fail(SARBP_ERR_PLAN, "node %d is not an external node", node);
     if ((uintptr_t)image & 7) return fail(SARBP_ERR_TYPE, "image must be 8-byte aligned");
     float2* arena = reinterpret_cast<float2*>(reinterpret_cast<char*>(plan->bound) + plan->arena_offset);
-    const cudaError_t e = cudaMemcpyAsync(arena + d.out_offset, image, (size_t)d.nr * d.nu * sizeof(float2),
-                                          cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+    const cudaError_t e = cudaMemcpy2DAsync(arena + d.out_offset, (size_t)d.out_stride * sizeof(float2), image,
+                                            (size_t)d.nu * sizeof(float2), (size_t)d.nu * sizeof(float2), (size_t)d.nr,
+                                            cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "set_node_image: %s", cudaGetErrorString(e));
     return SARBP_OK;
 }
@@ -683,6 +824,20 @@ int sarbp_ffbp_set_merge_queue(sarbp_ffbp_plan* plan, int on) {
     plan->launches = plan->mode == SARBP_SPLIT
                          ? 3 + 1 + (plan->max_height > 0 ? (plan->merge_queue ? 1 : plan->max_height) : 0)
                          : plan->max_height + 1;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_set_staging(sarbp_ffbp_plan* plan, int on) {
+    if (!plan) return fail(SARBP_ERR_TYPE, "plan must not be NULL");
+    if (on != 0 && on != 1) return fail(SARBP_ERR_VALUE, "on must be 0 or 1 (got %d)", on);
+    if (plan->bound) return fail(SARBP_ERR_PLAN, "set staging before sarbp_ffbp_bind");
+    plan->staging = on != 0;
+    return SARBP_OK;
+}
+
+int sarbp_ffbp_staging(const sarbp_ffbp_plan* plan, int* staged) {
+    if (!plan || !staged) return fail(SARBP_ERR_TYPE, "plan and staged must not be NULL");
+    *staged = plan->staged ? 1 : 0;
     return SARBP_OK;
 }
 
@@ -739,7 +894,9 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
             st = launch_split_ffbp_leaf_pulses(in, nodes, leaves, (int)plan->leaves.size(), precs, s);
         if (st == SARBP_OK)
             st = launch_split_ffbp_child_records(k, nodes, tables, items + plan->stage_begin[0] + plan->stage_count[0],
-                                                 (int)plan->merge_items, arena, crecs, s);
+                                                 (int)plan->merge_items, arena,
+                                                 plan->staged && !plan->merge_queue ? base + plan->tmap_offset : nullptr,
+                                                 crecs, s);
         if (st == SARBP_OK)
             st = launch_split_ffbp_leaves(in, nodes, items + plan->stage_begin[0], plan->stage_count[0], ch, wb,
                                           tables, precs, arena, root_out, 0, s);
@@ -765,7 +922,7 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
             const size_t first = (size_t)(plan->stage_begin[h] - plan->stage_begin[1]);
             st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables,
                                           reinterpret_cast<char*>(crecs) + 2 * first * crec_size, arena, root_out, 0,
-                                          s);
+                                          plan->staged ? plan->merge_box_bytes[h] : 0, s);
         }
     } else {
         const int2* blocks = reinterpret_cast<const int2*>(base + plan->node_bytes);

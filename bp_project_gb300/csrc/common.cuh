@@ -99,6 +99,11 @@ struct PolarDesc {
     // The FP64 geometry as two-float pairs (hi, lo), split on the host, so that per-tile set-up
     // on the GPU needs no FP64: origin x/y/z, r0, dr, u0, du, 1/dr, 1/du.
     float2 tf[9];
+    // FFBP children in split mode: the rectangle of this node's image that a merge tile of its
+    // parent reads, staged in shared memory by one TMA copy per tile.  It starts box_r rows and
+    // box_u columns (then rounded down to an even column) before the stencil bin of the parent
+    // tile's centre pixel and is box_h x box_w elements; box_w == 0: not staged.
+    int box_r, box_u, box_h, box_w;
 };
 
 // Fills PolarDesc::tf from the FP64 fields (host).
@@ -258,8 +263,10 @@ int launch_split_ffbp_tables(const PulseInputs& in, const PolarDesc* nodes, int 
                              float4* tables, cudaStream_t s);
 int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes, const int* leaves, int n_leaves,
                                   void* recs, cudaStream_t s);
+// tmaps: per node a 128-byte TMA tensor map of its image (used for children with box_w > 0), or
+// NULL (no staging: the merge tiles gather from global memory).
 int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const float4* tables, const TileItem* items,
-                                    int n_items, float2* arena, void* recs, cudaStream_t s);
+                                    int n_items, float2* arena, const void* tmaps, void* recs, cudaStream_t s);
 size_t split_ffbp_pulse_record_bytes();
 size_t split_ffbp_child_record_bytes();
 int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, const TileItem* items, int nitems,
@@ -277,8 +284,17 @@ struct MergeQueue {
 int launch_split_ffbp_merge_queue(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                                   const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
                                   const MergeQueue& Q, cudaStream_t s);
+// box_bytes > 0: the level's child records carry tensor maps, and each merge tile stages its two
+// children's footprints (at most box_bytes of shared memory together) by TMA.
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                              const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
-                             cudaStream_t s);
+                             size_t box_bytes, cudaStream_t s);
+// Shared-memory bytes of one staged child footprint (rows x cols complex64, 128-byte granules).
+__host__ __device__ inline size_t split_box_bytes(int rows, int cols) { return ((size_t)rows * cols * 8 + 127) / 128 * 128; }
+// Largest staged footprint per child: with two of them, the tables, the alignment slack and the
+// static shared memory a merge CTA stays within 28 KB, so eight fit an SM's 228 KB.
+constexpr size_t kMaxChildBox = 9728;
+// Tensor-map bytes per node.
+constexpr size_t kTensorMapBytes = 128;
 
 }  // namespace sarbp

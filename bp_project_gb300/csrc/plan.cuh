@@ -39,6 +39,12 @@ struct sarbp_ffbp_plan {
     size_t queue_offset = 0, queue_bytes = 0;
     unsigned long long queue_limit_ns = 5000000000ull;  // wait limit per merge item
     int withheld = -1;            // a node that never becomes ready (tests of the wait limit), or -1
+    // Split: merge tiles stage their children's footprints in shared memory by TMA, through one
+    // tensor map per child image (encoded at bind).  staging: requested (default on); staged:
+    // the tensor maps were encoded at the last bind.
+    bool staging = true, staged = false;
+    std::vector<size_t> merge_box_bytes;  // per height: a merge tile's footprint bytes (0: not staged)
+    size_t tmap_offset = 0, tmap_bytes = 0;
 };
 
 // Range extent (m) of the tallest leaf tile of a split plan: the leaf kernel's range window per

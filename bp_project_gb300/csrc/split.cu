@@ -974,14 +974,8 @@ __device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* s
     return make_float2(ar, ai);
 }
 
-#if SARBP_BULK_WINDOWS
-__device__ int g_bulk_timeouts;  // bulk-copy waits that ran out (the staged windows are then invalid)
+__device__ int g_wait_timeouts;  // bounded waits on asynchronous copies that ran out
 
-// Raw samples [b - 1, b + cnt + 2) of each fitting pulse's row (clipped to the row) arrive in
-// shared memory by one 1-D cp.async.bulk copy per pulse, issued by warp 0 after lane 0 has set
-// the transaction count on the mbarrier; every thread waits for the phase (a bounded wait that
-// records a timeout), then the Horner transform reads shared memory.  A copy must start and end
-// on 16-byte boundaries of the data array, so the copied range is widened to even elements.
 // Bounded wait for the phase `phase` of the mbarrier at shared address bar; true once it completed.
 __device__ __forceinline__ bool bulk_wait(unsigned bar, unsigned phase) {
     unsigned done = 0;
@@ -994,6 +988,12 @@ __device__ __forceinline__ bool bulk_wait(unsigned bar, unsigned phase) {
     return done != 0;
 }
 
+#if SARBP_BULK_WINDOWS
+// Raw samples [b - 1, b + cnt + 2) of each fitting pulse's row (clipped to the row) arrive in
+// shared memory by one 1-D cp.async.bulk copy per pulse, issued by warp 0 after lane 0 has set
+// the transaction count on the mbarrier; every thread waits for the phase (a bounded wait that
+// records a timeout), then the Horner transform reads shared memory.  A copy must start and end
+// on 16-byte boundaries of the data array, so the copied range is widened to even elements.
 // Returns false (the same in every thread) if the copies did not arrive within the bounded wait;
 // the caller then stops staging and waits once more before leaving.
 __device__ __forceinline__ bool bulk_stage_windows(const SplitParams& P, TileShared& S, const Rec* rec, float4* win,
@@ -1061,7 +1061,7 @@ __device__ __forceinline__ bool bulk_stage_windows(const SplitParams& P, TileSha
     // Bounded wait for the copies of this chunk's phase.
     const bool done = __syncthreads_and(bulk_wait(bar, phase)) != 0;  // also orders roff / raw0 of warp 0
     if (!done) {
-        if (threadIdx.x == 0) atomicAdd(&g_bulk_timeouts, 1);
+        if (threadIdx.x == 0) atomicAdd(&g_wait_timeouts, 1);
         return false;
     }
     for (int nl = warp; nl < nfit; nl += kThreads / 32) {
@@ -1139,7 +1139,7 @@ __device__ void chunk_loop(const SplitParams& P, const Job& J, TileShared& S, ch
 #if SARBP_BULK_WINDOWS
             if (bulk) {
                 if (!bulk_stage_windows(P, S, rec, win, raw, mbar, phase, c0, nfit, weighted)) {
-                    // The copies did not arrive: the tile's image is invalid (g_bulk_timeouts counts it).
+                    // The copies did not arrive: the tile's image is invalid (g_wait_timeouts counts it).
                     // Wait once more, bounded, for the copies still in flight, then leave.
                     bulk_wait((unsigned)__cvta_generic_to_shared(&mbar), phase);
                     break;
@@ -2215,6 +2215,10 @@ struct ChildRec {
     float inv_sdr, inv_sdu;
     int ir0, iu0, snr, snu;
     const float2* img;
+    int sstr;           // row stride of the child image (elements)
+    int br0, bu0;       // staged footprint: first row and (even) first column in the child image
+    int bh, bw;         // footprint rows and columns; bw == 0: not staged
+    const void* tmap;   // TMA tensor map of the child image (staged footprints only)
 };
 
 // Record of a polar image c seen from the ground point (px, py, 0), in two-float FP32
@@ -2256,18 +2260,24 @@ __device__ __forceinline__ ChildRec child_rec_at(FF K, float scale_w, float inv_
     R.snr = c.nr;
     R.snu = c.nu;
     R.img = img;
+    R.sstr = (int)c.out_stride;
+    R.br0 = R.bu0 = R.bh = R.bw = 0;
+    R.tmap = nullptr;
     return R;
 }
 
 // One thread per (merge tile, child).  The tile centre is the centre pixel's position from
 // the node's row and column tables (two-float g and c, u), the same point setup_polar_tab
-// measures the pixel offsets from.
+// measures the pixel offsets from.  With tensor maps (tmaps != NULL) a child whose node has a
+// footprint box gets the box's origin in its image: box_r rows and box_u columns (rounded down
+// to an even column, the TMA's 16-byte rule for 8-byte elements) before the centre's bin.
 __device__ __forceinline__ void child_record(FF K, float scale_w, float inv_scale_w,
                                              const PolarDesc* __restrict__ nodes, const float4* __restrict__ tables,
                                              const TileItem it, int t, float2* __restrict__ arena,
-                                             ChildRec* __restrict__ out) {
+                                             const void* tmaps, ChildRec* __restrict__ out) {
     const PolarDesc& g = nodes[it.node];
-    const PolarDesc& c = nodes[(t & 1) ? g.right : g.left];
+    const int ci = (t & 1) ? g.right : g.left;
+    const PolarDesc& c = nodes[ci];
     const int cols_t = 1 << g.tile_lc, rows_t = kSplitTilePixels >> g.tile_lc;
     const int i0 = min(g.win_r0 + it.tile_r + (rows_t >> 1), g.nr - 1);
     const int j0 = min(g.win_u0 + it.tile_u + (cols_t >> 1), g.nu - 1);
@@ -2279,16 +2289,23 @@ __device__ __forceinline__ void child_record(FF K, float scale_w, float inv_scal
     const FF py = ff_add(ff_of(g.tf[1]), ff_mul(g0, FF{cv.z, cv.w}));
     ChildRec R = child_rec_at(K, scale_w, inv_scale_w, c, px, py, arena + c.out_offset);
     if (!(t & 1)) tab_quantum(g, g.tile_lc, it.tile_r, it.tile_u, tables, R.d.z, R.d.w);
+    if (tmaps != nullptr && c.box_w > 0 && R.ir0 > -(1 << 30)) {
+        R.br0 = R.ir0 - c.box_r;
+        R.bu0 = (R.iu0 - c.box_u) & ~1;
+        R.bh = c.box_h;
+        R.bw = c.box_w;
+        R.tmap = static_cast<const char*>(tmaps) + kTensorMapBytes * (size_t)ci;
+    }
     out[t] = R;
 }
 
 __global__ void ffbp_child_records_kernel(float Kh, float Kl, float scale_w, float inv_scale_w,
                                           const PolarDesc* __restrict__ nodes, const float4* __restrict__ tables,
                                           const TileItem* __restrict__ items, int n_items,
-                                          float2* __restrict__ arena, ChildRec* __restrict__ out) {
+                                          float2* __restrict__ arena, const void* tmaps, ChildRec* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * n_items) return;
-    child_record(FF{Kh, Kl}, scale_w, inv_scale_w, nodes, tables, items[t >> 1], t, arena, out);
+    child_record(FF{Kh, Kl}, scale_w, inv_scale_w, nodes, tables, items[t >> 1], t, arena, tmaps, out);
 }
 
 // Child-image coordinates of a parent pixel: bin indices (ir, iu), centred fractions
@@ -2332,10 +2349,10 @@ __device__ __forceinline__ float2 child_value(float Kf, const ChildRec& R, const
         float wr[4], wu[4];
         lagrange_centred(c.sr, wr);
         lagrange_centred(c.su, wu);
-        const float2* base = R.img + (size_t)(c.ir - 1) * R.snu + (c.iu - 1);
+        const float2* base = R.img + (size_t)(c.ir - 1) * R.sstr + (c.iu - 1);
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            const float2* row = base + (size_t)a * R.snu;
+            const float2* row = base + (size_t)a * R.sstr;
             const float2 x0 = __ldg(row), x1 = __ldg(row + 1), x2 = __ldg(row + 2), x3 = __ldg(row + 3);
             float rr = wu[0] * x0.x, ri = wu[0] * x0.y;
             rr = fmaf(wu[1], x1.x, rr);
@@ -2377,6 +2394,8 @@ struct __align__(16) ChildDup {
     float2 cx;         // Phi
     int ir0, iu0, snr, snu;
     const float2* img;
+    int sstr;          // row stride of the child image
+    int xr0, xu0, xh, xw;  // staged footprint: first row, first column, rows, columns (xw == 0: not staged)
 };
 
 __device__ __forceinline__ void child_dup_store(const ChildRec& R, ChildDup& P) {
@@ -2402,6 +2421,11 @@ __device__ __forceinline__ void child_dup_store(const ChildRec& R, ChildDup& P) 
     P.snr = R.snr;
     P.snu = R.snu;
     P.img = R.img;
+    P.sstr = R.sstr;
+    P.xr0 = R.br0;
+    P.xu0 = R.bu0;
+    P.xh = R.bh;
+    P.xw = R.bw;
 }
 
 // Offsets of the parent pixels (row, col) and (row + 1, col) from the tile centre as (upper,
@@ -2426,21 +2450,28 @@ __device__ __forceinline__ VPix tab_vpair(const TabF& T, int row, int col) {
     return v;
 }
 
-// 4x4 Lagrange stencil of one child at bin (ir, iu) with weights wr (range) and wu (angle);
-// (re, im) run as one f32x2 pair.
-// COHERENT: the child image was written by other CTAs of the same launch (the merge queue), so it
-// is read with weak ld.global (L1-cached, ordered by the acquire that made the node ready) instead
-// of the read-only path.  The asm has no memory clobber, so the compiler schedules it as freely as
-// __ldg; its address comes from values read after the CTA barrier that follows the acquire.
-template <bool COHERENT>
+// Where a stencil's taps come from: the child image through the read-only path (kLdg), the
+// child image with weak coherent loads (kCoherent: the merge queue, whose child images were
+// written by other CTAs of the same launch; L1-cached, ordered by the acquire that made the
+// node ready), or the tile's staged footprint in shared memory (kShared).
+enum TapSource { kLdg = 0, kCoherent = 1, kShared = 2 };
+
+// The coherent asm has no memory clobber, so the compiler schedules it as freely as __ldg; its
+// address comes from values read after the CTA barrier that follows the acquire.
+template <int SRC>
 __device__ __forceinline__ void ld_child_row(const float2* p, float2& x0, float2& x1, float2& x2, float2& x3) {
-    if (COHERENT) {
+    if (SRC == kCoherent) {
         asm("ld.global.v2.f32 {%0, %1}, [%8];\n\t"
             "ld.global.v2.f32 {%2, %3}, [%8+8];\n\t"
             "ld.global.v2.f32 {%4, %5}, [%8+16];\n\t"
             "ld.global.v2.f32 {%6, %7}, [%8+24];"
             : "=f"(x0.x), "=f"(x0.y), "=f"(x1.x), "=f"(x1.y), "=f"(x2.x), "=f"(x2.y), "=f"(x3.x), "=f"(x3.y)
             : "l"(p));
+    } else if (SRC == kShared) {
+        x0 = p[0];
+        x1 = p[1];
+        x2 = p[2];
+        x3 = p[3];
     } else {
         x0 = __ldg(p);
         x1 = __ldg(p + 1);
@@ -2449,16 +2480,15 @@ __device__ __forceinline__ void ld_child_row(const float2* p, float2& x0, float2
     }
 }
 
-template <bool COHERENT>
-__device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, int snu, int ir, int iu,
-                                                const float wr[4], const float wu[4]) {
-    const float2* base = img + (size_t)(ir - 1) * snu + (iu - 1);
+// 4x4 Lagrange stencil whose first tap is base (rows `stride` elements apart) with weights wr
+// (range) and wu (angle); (re, im) run as one f32x2 pair.
+template <int SRC>
+__device__ __forceinline__ float2 child_stencil(const float2* base, int stride, const float wr[4], const float wu[4]) {
     float2 v = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        const float2* row = base + (size_t)a * snu;
         float2 x0, x1, x2, x3;
-        ld_child_row<COHERENT>(row, x0, x1, x2, x3);
+        ld_child_row<SRC>(base + (size_t)a * stride, x0, x1, x2, x3);
         float2 r = __fmul2_rn(pair(wu[0]), x0);
         r = __ffma2_rn(pair(wu[1]), x1, r);
         r = __ffma2_rn(pair(wu[2]), x2, r);
@@ -2468,6 +2498,34 @@ __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, 
     return v;
 }
 
+// The two stencils of a vertical pair that share three rows: one 5x4 block from row (base),
+// the upper pixel's stencil in rows 0-3, the lower one's in rows 1-4 (the same sums as
+// child_stencil per pixel).
+template <int SRC>
+__device__ __forceinline__ void child_pair_block(const float2* base, int stride, const float wrA[4],
+                                                 const float wuA[4], const float wrB[4], const float wuB[4],
+                                                 float2& vA, float2& vB) {
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+        float2 x0, x1, x2, x3;
+        ld_child_row<SRC>(base + (size_t)a * stride, x0, x1, x2, x3);
+        if (a < 4) {
+            float2 r = __fmul2_rn(pair(wuA[0]), x0);
+            r = __ffma2_rn(pair(wuA[1]), x1, r);
+            r = __ffma2_rn(pair(wuA[2]), x2, r);
+            r = __ffma2_rn(pair(wuA[3]), x3, r);
+            vA = __ffma2_rn(pair(wrA[a]), r, vA);
+        }
+        if (a > 0) {
+            float2 r = __fmul2_rn(pair(wuB[0]), x0);
+            r = __ffma2_rn(pair(wuB[1]), x1, r);
+            r = __ffma2_rn(pair(wuB[2]), x2, r);
+            r = __ffma2_rn(pair(wuB[3]), x3, r);
+            vB = __ffma2_rn(pair(wrB[a - 1]), r, vB);
+        }
+    }
+}
+
 // Child C at the column pair q (lanes: the upper and the lower parent pixel), rotated: per lane
 // child_value's arithmetic (the Lagrange weights, the stencil's sum order and the rotation are
 // the same).  Two vertically adjacent parent pixels nearly always fall one child range bin apart
@@ -2475,8 +2533,15 @@ __device__ __forceinline__ float2 child_stencil(const float2* __restrict__ img, 
 // cosine of the angle between the two phase centres' lines of sight), so their 4x4 stencils
 // share three rows: when that holds for every lane of the warp, the pair gathers one 5x4 block
 // (20 loads instead of 32).  Otherwise each pixel gathers its own stencil.
-template <bool COHERENT>
-__device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const VPix& q, float2& oA, float2& oB) {
+// sbox (STAGED, not NULL): the child's footprint staged in shared memory (C.xh x C.xw elements
+// from row C.xr0, column C.xu0); a warp whose pairs all share a block inside it reads the blocks
+// from shared memory, any other warp gathers each pixel's stencil from the child image (staged
+// kernels have no other paths: fewer code paths keep their loop in the instruction cache).  The
+// taps are the same values either way.
+template <bool COHERENT, bool STAGED>
+__device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const VPix& q, float2& oA, float2& oB,
+                                            const float2* sbox) {
+    constexpr int SRC = COHERENT ? kCoherent : kLdg;
     const float2 magic = pair(kMagic), nmagic = pair(-kMagic), mone = pair(-1.0f);
     const float2 nL = __ffma2_rn(C.nbx, q.dx, __fmul2_rn(C.nby, q.dy));
     const float2 nq2 = __ffma2_rn(nL, nL, q.nd2);
@@ -2516,45 +2581,37 @@ __device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const V
     const int iuA = C.iu0 + (__float_as_int(tu.x) - kMagicBits), iuB = C.iu0 + (__float_as_int(tu.y) - kMagicBits);
     const bool okA = irA >= 1 && irA <= C.snr - 3 && iuA >= 1 && iuA <= C.snu - 3 && gp.x > 0.0f;
     const bool okB = irB >= 1 && irB <= C.snr - 3 && iuB >= 1 && iuB <= C.snu - 3 && gp.y > 0.0f;
+    const bool share = okA && okB && irB == irA + 1 && iuB == iuA;
     float2 vA = make_float2(0.0f, 0.0f), vB = vA;
-    if (__all_sync(0xffffffffu, okA && okB && irB == irA + 1 && iuB == iuA)) {
+    // The pair's block origin relative to the staged footprint (at least 8 x 8 elements when staged).
+    const int rA = irA - 1 - C.xr0, uA = iuA - 1 - C.xu0;
+    if (STAGED && sbox != nullptr && __all_sync(0xffffffffu, share && (unsigned)rA <= (unsigned)(C.xh - 5) &&
+                                              (unsigned)uA <= (unsigned)(C.xw - 4))) {
         float wrA[4], wuA[4], wrB[4], wuB[4];
         lagrange_centred(sr.x, wrA);
         lagrange_centred(su.x, wuA);
         lagrange_centred(sr.y, wrB);
         lagrange_centred(su.y, wuB);
-        const float2* row = C.img + (size_t)(irA - 1) * C.snu + (iuA - 1);
-#pragma unroll
-        for (int a = 0; a < 5; ++a) {
-            float2 x0, x1, x2, x3;
-            ld_child_row<COHERENT>(row + (size_t)a * C.snu, x0, x1, x2, x3);
-            if (a < 4) {
-                float2 r = __fmul2_rn(pair(wuA[0]), x0);
-                r = __ffma2_rn(pair(wuA[1]), x1, r);
-                r = __ffma2_rn(pair(wuA[2]), x2, r);
-                r = __ffma2_rn(pair(wuA[3]), x3, r);
-                vA = __ffma2_rn(pair(wrA[a]), r, vA);
-            }
-            if (a > 0) {
-                float2 r = __fmul2_rn(pair(wuB[0]), x0);
-                r = __ffma2_rn(pair(wuB[1]), x1, r);
-                r = __ffma2_rn(pair(wuB[2]), x2, r);
-                r = __ffma2_rn(pair(wuB[3]), x3, r);
-                vB = __ffma2_rn(pair(wrB[a - 1]), r, vB);
-            }
-        }
+        child_pair_block<kShared>(sbox + rA * C.xw + uA, C.xw, wrA, wuA, wrB, wuB, vA, vB);
+    } else if (!STAGED && __all_sync(0xffffffffu, share)) {
+        float wrA[4], wuA[4], wrB[4], wuB[4];
+        lagrange_centred(sr.x, wrA);
+        lagrange_centred(su.x, wuA);
+        lagrange_centred(sr.y, wrB);
+        lagrange_centred(su.y, wuB);
+        child_pair_block<SRC>(C.img + (size_t)(irA - 1) * C.sstr + (iuA - 1), C.sstr, wrA, wuA, wrB, wuB, vA, vB);
     } else {
         if (okA) {
             float wr[4], wu[4];
             lagrange_centred(sr.x, wr);
             lagrange_centred(su.x, wu);
-            vA = child_stencil<COHERENT>(C.img, C.snu, irA, iuA, wr, wu);
+            vA = child_stencil<SRC>(C.img + (size_t)(irA - 1) * C.sstr + (iuA - 1), C.sstr, wr, wu);
         }
         if (okB) {
             float wr[4], wu[4];
             lagrange_centred(sr.y, wr);
             lagrange_centred(su.y, wu);
-            vB = child_stencil<COHERENT>(C.img, C.snu, irB, iuB, wr, wu);
+            vB = child_stencil<SRC>(C.img + (size_t)(irB - 1) * C.sstr + (iuB - 1), C.sstr, wr, wu);
         }
     }
     // (vr cs - vi sn, vr sn + vi cs)
@@ -2562,16 +2619,49 @@ __device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const V
     oB = __ffma2_rn(pair(vB.x), make_float2(csB, snB), __fmul2_rn(pair(vB.y), make_float2(-snB, csB)));
 }
 
+// Bytes of a merge tile's tables in dynamic shared memory (the staged footprints follow them).
+constexpr int kTabBytes = (int)((sizeof(TabF) + 127) / 128 * 128);
+
+// Staged merge tiles: one thread starts the TMA copies of both children's footprints (2-D tiles
+// of the child images, the box's first column even so that it starts on a 16-byte boundary;
+// rows or columns outside the image arrive as zeros and are never read, since such stencils
+// fail the bounds test) with completion on one mbarrier.  Child 1's footprint follows child 0's
+// at the next 128-byte boundary.
+__device__ __forceinline__ void stage_children(const ChildRec* __restrict__ crec, unsigned box0, unsigned bar) {
+    const int bw0 = crec[0].bw, bw1 = crec[1].bw;
+    const unsigned b0 = bw0 > 0 ? (unsigned)(crec[0].bh * bw0 * 8) : 0u;
+    const unsigned b1 = bw1 > 0 ? (unsigned)(crec[1].bh * bw1 * 8) : 0u;
+    if (b0 + b1 == 0) return;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(b0 + b1) : "memory");
+    if (b0)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+            ::"r"(box0), "l"(crec[0].tmap), "r"(crec[0].bu0), "r"(crec[0].br0), "r"(bar)
+            : "memory");
+    if (b1)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+            ::"r"(box0 + (b0 + 127u) / 128u * 128u), "l"(crec[1].tmap), "r"(crec[1].bu0), "r"(crec[1].br0), "r"(bar)
+            : "memory");
+}
+
 // One merge tile: both children regridded onto the parent tile, each rounded to complex64,
 // then added (the reference's rounding points).  crec points at the tile's two child records.
 // Thread t of THREADS forms the column pairs (rows 2 m and 2 m + 1 of column t mod cols) for
 // m = t / cols + i THREADS / cols; its offsets come back from the shared tables per pair, which
 // keeps the live state small.
-template <bool COHERENT = false, int THREADS = kThreads>
+// STAGED: smem is 128-byte aligned and holds [tables | child 0's footprint | child 1's], which
+// stage_children's copies fill (completion on the mbarrier at shared address bar).  Each warp
+// waits for them (bounded); a warp whose wait runs out counts a timeout and gathers from the
+// child images instead, and the tile waits once more before it ends, so that no copy into its
+// shared memory is still in flight when the CTA exits.
+template <bool COHERENT = false, int THREADS = kThreads, bool STAGED = false>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
                                            ChildDup* C, float2* __restrict__ arena, float2* root_out, int root,
-                                           char* smem) {
+                                           char* smem, unsigned bar = 0) {
     Job J;
     J.g = nodes[it.node];
     J.lc = J.g.tile_lc;
@@ -2581,17 +2671,33 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     const float4 d0 = __ldg(&crec[0].d);  // (G, frac(Qu) - 1/2, tile quantum, its inverse)
     TabF& T = *reinterpret_cast<TabF*>(smem);
     setup_polar_tab<THREADS>(J, T, tables, d0.z, d0.w);
+    const float2* sbox[2] = {nullptr, nullptr};
+    bool waited = true;
+    if (STAGED && (C[0].xw > 0 || C[1].xw > 0)) {
+        waited = __all_sync(0xffffffffu, bulk_wait(bar, 0));
+        if (!waited) {
+            if ((threadIdx.x & 31) == 0) atomicAdd(&g_wait_timeouts, 1);
+        } else {
+            const float2* b0 = reinterpret_cast<const float2*>(smem + kTabBytes);
+            if (C[0].xw > 0) sbox[0] = b0;
+            if (C[1].xw > 0)
+                sbox[1] = b0 + (C[0].xw > 0 ? (int)split_box_bytes(C[0].xh, C[0].xw) / 8 : 0);
+        }
+    }
     float2* dst = J.g.dst ? J.g.dst : (it.node == root ? root_out : arena + J.g.out_offset);
     const int col = threadIdx.x & ((1 << J.lc) - 1), wu = J.tile_u + col;
     constexpr int kPairs = kSplitTilePixels / (2 * THREADS);  // column pairs per thread
     float2 m[2 * kPairs];
-#pragma unroll
+    // Gathering tiles keep all their pairs' gathers in flight (unrolled); staged tiles read shared
+    // memory with short latency, and the smaller loop body keeps their instruction cache warm.
+    constexpr int kUnroll = STAGED ? 1 : kPairs;
+#pragma unroll kUnroll
     for (int k = 0; k < kPairs; ++k) {
         const int row = 2 * ((threadIdx.x >> J.lc) + (THREADS >> J.lc) * k);
         const VPix v = tab_vpair(T, row, col);
         float2 a0, b0, a1, b1;
-        child_vpair<COHERENT>(Kf, C[0], v, a0, b0);
-        child_vpair<COHERENT>(Kf, C[1], v, a1, b1);
+        child_vpair<COHERENT, STAGED>(Kf, C[0], v, a0, b0, sbox[0]);
+        child_vpair<COHERENT, STAGED>(Kf, C[1], v, a1, b1, sbox[1]);
         const float2 mA = __fadd2_rn(a0, a1), mB = __fadd2_rn(b0, b1);
         if (!COHERENT) {
             const int wr = J.tile_r + row;
@@ -2616,6 +2722,7 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
             }
         }
     }
+    if (STAGED && !waited) bulk_wait(bar, 0);  // the copies may still land: not past the CTA's end
 }
 
 __global__ void __launch_bounds__(kMergeThreads, 8) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
@@ -2628,6 +2735,28 @@ __global__ void __launch_bounds__(kMergeThreads, 8) split_merge_kernel(SplitPara
     __shared__ ChildDup C[2];
     merge_tile<false, kMergeThreads>(P.Kf, nodes, items[blockIdx.x], tables, crecs + 2 * (long long)blockIdx.x, C, arena,
                                      root_out, root, smem);
+}
+
+// The merge with both children's footprints staged in shared memory by TMA (tiles whose child
+// records carry tensor maps; any other child gathers from its image as in split_merge_kernel).
+// The dynamic shared memory is 128 bytes of alignment slack, the tables and the footprints.
+__global__ void __launch_bounds__(kMergeThreads, 8) split_merge_staged_kernel(SplitParams P,
+                                                                         const PolarDesc* __restrict__ nodes,
+                                                                         const TileItem* __restrict__ items,
+                                                                         const float4* __restrict__ tables,
+                                                                         const ChildRec* __restrict__ crecs,
+                                                                         float2* __restrict__ arena,
+                                                                         float2* root_out, int root) {
+    extern __shared__ __align__(128) char smem_raw[];
+    __shared__ ChildDup C[2];
+    __shared__ __align__(8) unsigned long long mbar;
+    const unsigned raw = (unsigned)__cvta_generic_to_shared(smem_raw);
+    char* smem = smem_raw + (((raw + 127u) & ~127u) - raw);
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&mbar);
+    const ChildRec* crec = crecs + 2 * (long long)blockIdx.x;
+    if (threadIdx.x == 0) stage_children(crec, (unsigned)__cvta_generic_to_shared(smem + kTabBytes), bar);
+    merge_tile<false, kMergeThreads, true>(P.Kf, nodes, items[blockIdx.x], tables, crec, C, arena, root_out, root,
+                                           smem, bar);
 }
 
 // All merge levels in one persistent launch.  Items are in height order; a CTA claims the next
@@ -2852,19 +2981,15 @@ int launch_split_polar(const PulseInputs& in, const PolarDesc& g, int pulse_spli
     return check_launch("split_polar");
 }
 
-// The pulse split of a direct lattice launch that asks for the automatic one: sized for the
-// largest window budget, so that it depends on the lattice only and the workspace query and the
-// launch agree (fewer pulses only lower it).
 int split_wait_timeouts(int* count) {
-#if SARBP_BULK_WINDOWS
-    const cudaError_t e = cudaMemcpyFromSymbol(count, g_bulk_timeouts, sizeof(int));
+    const cudaError_t e = cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(int));
     if (e != cudaSuccess) return fail(SARBP_ERR_CUDA, "wait timeouts: %s", cudaGetErrorString(e));
-#else
-    *count = 0;
-#endif
     return SARBP_OK;
 }
 
+// The pulse split of a direct lattice launch that asks for the automatic one: sized for the
+// largest window budget, so that it depends on the lattice only and the workspace query and the
+// launch agree (fewer pulses only lower it).
 int split_lattice_auto_split(const sarbp_lattice& lat, int pulses) {
     const size_t smem = dynamic_smem(capacity_for(kMaxChunk, 1 << 20, kLatticeWindowBudget), false);
     if (prepare(split_lattice_kernel, smem) != SARBP_OK) return 1;
@@ -2939,14 +3064,14 @@ int launch_split_ffbp_leaf_pulses(const PulseInputs& in, const PolarDesc* nodes,
 }
 
 int launch_split_ffbp_child_records(double k, const PolarDesc* nodes, const float4* tables, const TileItem* items,
-                                    int n_items, float2* arena, void* recs, cudaStream_t s) {
+                                    int n_items, float2* arena, const void* tmaps, void* recs, cudaStream_t s) {
     if (n_items <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
     none.data_dr = 1.0;
     const SplitParams P = make_params(none, 1, 4, 1);
     ffbp_child_records_kernel<<<grid_blocks(2LL * n_items, kThreads), kThreads, 0, s>>>(
-        P.Kh, P.Kl, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, items, n_items, arena,
+        P.Kh, P.Kl, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, items, n_items, arena, tmaps,
         reinterpret_cast<ChildRec*>(recs));
     note_launches(1);
     return check_launch("split_ffbp_child_records");
@@ -2970,12 +3095,20 @@ int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, cons
 
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                              const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
-                             cudaStream_t s) {
+                             size_t box_bytes, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
     none.data_dr = 1.0;
     SplitParams P = make_params(none, 1, 4, 1);
+    if (box_bytes > 0) {
+        const size_t smem = 128 + kTabBytes + box_bytes;
+        if (int st = prepare(split_merge_staged_kernel, smem)) return st;
+        split_merge_staged_kernel<<<nitems, kMergeThreads, smem, s>>>(
+            P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs), arena, root_out, root);
+        note_launches(1);
+        return check_launch("split_ffbp_merges (staged)");
+    }
     const size_t smem = merge_smem();
     if (int st = prepare(split_merge_kernel, smem)) return st;
     split_merge_kernel<<<nitems, kMergeThreads, smem, s>>>(P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs),
@@ -3189,7 +3322,7 @@ __global__ void batch_child_records_kernel(const BatchScene* __restrict__ scenes
     if (t >= 2 * n_items) return;
     const TileItem it = items[t >> 1];
     const SplitParams& P = scenes[it.pad].P;
-    child_record(FF{P.Kh, P.Kl}, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, it, t, arena, out);
+    child_record(FF{P.Kh, P.Kl}, (float)P.scale_w, (float)P.inv_scale_w, nodes, tables, it, t, arena, nullptr, out);
 }
 
 }  // namespace

@@ -344,6 +344,16 @@ int sarbp_ffbp_set_node_image(const sarbp_ffbp_plan* plan, int node, const float
  * launch per tree height, which measured faster.  The images are the same bit for bit.  No
  * counterpart in the reference (its levels are separate launches). */
 int sarbp_ffbp_set_merge_queue(sarbp_ffbp_plan* plan, int on);
+/* on = 1 (the default): the merge tiles of a split plan stage each child's footprint (the child
+ * stencil rows and columns the tile reads) in shared memory with one TMA tensor copy per child,
+ * through a tensor map per child image that sarbp_ffbp_bind encodes; on = 0: the tiles gather
+ * from the child images in global memory.  Set before sarbp_ffbp_bind.  The images are the same
+ * bit for bit.  Replaces the global-memory stencil gathers of the reference's merges
+ * (fast_bp/gpu/kernels.cu:70-137 sample2, gpu/resident_kernels.cu:35-55). */
+int sarbp_ffbp_set_staging(sarbp_ffbp_plan* plan, int on);
+/* *staged = 1 if the bound plan's merges stage their footprints (staging requested and the
+ * driver's tensor-map encoder available at bind), else 0.  No counterpart in the reference. */
+int sarbp_ffbp_staging(const sarbp_ffbp_plan* plan, int* staged);
 /* The queue's wait limit per merge tile (default 5 s; (0, 60]) and, for tests of that limit, a merge
  * node whose children are never counted complete (withheld_node >= 0; -1 for none), so that its
  * tiles' waits run out.  Set before sarbp_ffbp_bind.  A wait that runs out stops the launch and sets
@@ -404,10 +414,12 @@ int sarbp_direct_polar_phase32(const float* data, int pulses, int samples, const
  * measured FP32 denominator of the back-projection kernels' roofline. */
 int sarbp_fp32_peak(int packed, int iters, double* tflops);
 
-/* Number of bounded waits in the library's kernels that ran out since it was loaded (no
- * counterpart in the reference); synchronises the device.  The only waiting kernels are those of
- * the bulk-copy window staging build (SARBP_BULK_WINDOWS): a tile whose range windows did not
- * arrive in time stops early, so its image is invalid; the default build never waits and reports 0. */
+/* Number of bounded waits on asynchronous copies in the library's kernels that ran out since it
+ * was loaded (no counterpart in the reference); synchronises the device.  The waiting kernels are
+ * the staged FFBP merges (a warp whose TMA footprints did not arrive in time gathers from the
+ * child images instead: the image is still right) and those of the bulk-copy window staging build
+ * (SARBP_BULK_WINDOWS: a tile whose range windows did not arrive in time stops early, so its image
+ * is invalid). */
 int sarbp_wait_timeouts(int* count);
 
 #ifdef __cplusplus

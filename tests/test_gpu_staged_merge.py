@@ -1,0 +1,66 @@
+"""FFBP merge tiles that stage each child's footprint in shared memory by TMA (the default in split
+mode) form the same image, bit for bit, as merge tiles that gather the stencils from the child
+images in global memory; no staging wait runs out."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from bp_project_gb300 import build
+    build.build()
+    from bp_project_gb300 import _native
+    _native.load()
+    return _native
+
+
+def _images(config, **scale):
+    from bp_project_gb300 import core, scenes
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    cfg = scenes.scaled(scenes.CONFIGS[config], **scale) if scale else scenes.CONFIGS[config]
+    sc = scenes.synthesize(cfg, device="cuda")
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (sc.data, sc.position, sc.weight, sc.phase)]
+    out = {}
+    for staging in (True, False):
+        prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split", staging=staging)
+        assert prog.staged == staging
+        for _ in range(2):  # a second execute reuses the tensor maps and the node images
+            out[staging] = prog.execute(*dev, sc.range_start, sc.data_dr, sc.k).clone()
+        prog.close()
+    torch.cuda.synchronize()
+    return out
+
+
+def _timeouts(lib):
+    n = ctypes.c_int(-1)
+    lib.check(lib.load().sarbp_wait_timeouts(ctypes.byref(n)))
+    return n.value
+
+
+@pytest.mark.parametrize("config,scale", [("c1", dict(pulses=1024, samples=4096, image_side=512)),
+                                          ("c2", dict(pulses=2048, samples=4096, image_side=512)),
+                                          ("c0", {})])
+def test_staged_merge_equals_gathered_merge(lib, config, scale):
+    before = _timeouts(lib)
+    out = _images(config, **scale)
+    assert torch.equal(out[True], out[False])
+    assert float(out[True].abs().max()) > 0
+    assert _timeouts(lib) == before
+
+
+@pytest.mark.slow
+def test_staged_merge_equals_gathered_merge_c1(lib):
+    """The 4096-pulse / 2048^2 plan (8 merge levels, footprints of 16 x 71 and 24-30 x 39 elements)."""
+    before = _timeouts(lib)
+    out = _images("c1")
+    assert torch.equal(out[True], out[False])
+    assert _timeouts(lib) == before
