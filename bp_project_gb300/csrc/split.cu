@@ -2450,6 +2450,21 @@ __device__ __forceinline__ VPix tab_vpair(const TabF& T, int row, int col) {
     return v;
 }
 
+// lagrange_centred for two fractions at once (the lanes of f32x2 operations), per lane the same
+// operations and roundings: -a/6, -c2 and -s are the scalar code's a/6, c2 and s negated (exact).
+__device__ __forceinline__ void lagrange_centred2(float2 s, float2 w[4]) {
+    const float2 a = __ffma2_rn(s, s, pair(-0.25f));
+    const float2 na6 = __fmul2_rn(a, pair(-1.0f / 6.0f));
+    const float2 b2 = __ffma2_rn(a, pair(0.5f), pair(-1.0f));
+    const float2 c1 = __fmul2_rn(pair(-1.5f), na6);
+    const float2 nc2 = __fmul2_rn(pair(-0.5f), b2);
+    const float2 ns = __fmul2_rn(s, pair(-1.0f));
+    w[0] = __ffma2_rn(na6, s, c1);
+    w[3] = __ffma2_rn(na6, ns, c1);
+    w[1] = __ffma2_rn(b2, s, nc2);
+    w[2] = __ffma2_rn(b2, ns, nc2);
+}
+
 // Where a stencil's taps come from: the child image through the read-only path (kLdg), the
 // child image with weak coherent loads (kCoherent: the merge queue, whose child images were
 // written by other CTAs of the same launch; L1-cached, ordered by the acquire that made the
@@ -2588,10 +2603,16 @@ __device__ __forceinline__ void child_vpair(float Kf, const ChildDup& C, const V
     if (STAGED && sbox != nullptr && __all_sync(0xffffffffu, share && (unsigned)rA <= (unsigned)(C.xh - 5) &&
                                               (unsigned)uA <= (unsigned)(C.xw - 4))) {
         float wrA[4], wuA[4], wrB[4], wuB[4];
-        lagrange_centred(sr.x, wrA);
-        lagrange_centred(su.x, wuA);
-        lagrange_centred(sr.y, wrB);
-        lagrange_centred(su.y, wuB);
+        float2 wr2[4], wu2[4];
+        lagrange_centred2(sr, wr2);  // both pixels' weights as lane pairs
+        lagrange_centred2(su, wu2);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            wrA[k] = wr2[k].x;
+            wrB[k] = wr2[k].y;
+            wuA[k] = wu2[k].x;
+            wuB[k] = wu2[k].y;
+        }
         child_pair_block<kShared>(sbox + rA * C.xw + uA, C.xw, wrA, wuA, wrB, wuB, vA, vB);
     } else if (!STAGED && __all_sync(0xffffffffu, share)) {
         float wrA[4], wuA[4], wrB[4], wuB[4];
