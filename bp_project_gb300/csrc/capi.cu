@@ -922,7 +922,8 @@ int sarbp_ffbp_execute(const sarbp_ffbp_plan* plan, const float* data, int pulse
             const size_t first = (size_t)(plan->stage_begin[h] - plan->stage_begin[1]);
             st = launch_split_ffbp_merges(k, nodes, items + plan->stage_begin[h], plan->stage_count[h], tables,
                                           reinterpret_cast<char*>(crecs) + 2 * first * crec_size, arena, root_out, 0,
-                                          plan->staged ? plan->merge_box_bytes[h] : 0, s);
+                                          plan->staged ? plan->merge_box_bytes[h] : 0, plan->queue_limit_ns,
+                                          plan->withheld, s);
         }
     } else {
         const int2* blocks = reinterpret_cast<const int2*>(base + plan->node_bytes);

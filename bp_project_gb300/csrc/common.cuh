@@ -285,10 +285,12 @@ int launch_split_ffbp_merge_queue(double k, const PolarDesc* nodes, const TileIt
                                   const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
                                   const MergeQueue& Q, cudaStream_t s);
 // box_bytes > 0: the level's child records carry tensor maps, and each merge tile stages its two
-// children's footprints (at most box_bytes of shared memory together) by TMA.
+// children's footprints (at most box_bytes of shared memory together) by TMA, each warp waiting
+// for them at most wait_ns; the tiles of node `withheld` (tests; -1 for none) declare 16 bytes more
+// than their copies deliver, so that their waits run out.
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                              const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
-                             size_t box_bytes, cudaStream_t s);
+                             size_t box_bytes, unsigned long long wait_ns, int withheld, cudaStream_t s);
 // Shared-memory bytes of one staged child footprint (rows x cols complex64, 128-byte granules).
 __host__ __device__ inline size_t split_box_bytes(int rows, int cols) { return ((size_t)rows * cols * 8 + 127) / 128 * 128; }
 // Largest staged footprint per child: with two of them, the tables, the alignment slack and the

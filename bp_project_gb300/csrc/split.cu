@@ -976,6 +976,29 @@ __device__ __noinline__ float2 slow_pixel(const SplitParams& P, const SlowRec* s
 
 __device__ int g_wait_timeouts;  // bounded waits on asynchronous copies that ran out
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for phase `phase` of the mbarrier at shared address bar, for at most limit_ns of the GPU's
+// timer (and at most 2^24 polls); true once the phase completed.
+__device__ __forceinline__ bool timed_wait(unsigned bar, unsigned phase, unsigned long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    for (int it = 0; it < (1 << 24); ++it) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+    return false;
+}
+
 // Bounded wait for the phase `phase` of the mbarrier at shared address bar; true once it completed.
 __device__ __forceinline__ bool bulk_wait(unsigned bar, unsigned phase) {
     unsigned done = 0;
@@ -2647,15 +2670,18 @@ constexpr int kTabBytes = (int)((sizeof(TabF) + 127) / 128 * 128);
 // of the child images, the box's first column even so that it starts on a 16-byte boundary;
 // rows or columns outside the image arrive as zeros and are never read, since such stencils
 // fail the bounds test) with completion on one mbarrier.  Child 1's footprint follows child 0's
-// at the next 128-byte boundary.
-__device__ __forceinline__ void stage_children(const ChildRec* __restrict__ crec, unsigned box0, unsigned bar) {
+// at the next 128-byte boundary.  withhold: bytes declared on the mbarrier beyond those the copies
+// deliver (0; 16 in tests of the wait limit, whose phase then never completes).
+__device__ __forceinline__ void stage_children(const ChildRec* __restrict__ crec, unsigned box0, unsigned bar,
+                                               unsigned withhold) {
     const int bw0 = crec[0].bw, bw1 = crec[1].bw;
     const unsigned b0 = bw0 > 0 ? (unsigned)(crec[0].bh * bw0 * 8) : 0u;
     const unsigned b1 = bw1 > 0 ? (unsigned)(crec[1].bh * bw1 * 8) : 0u;
     if (b0 + b1 == 0) return;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(b0 + b1) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(b0 + b1 + withhold)
+                 : "memory");
     if (b0)
         asm volatile(
             "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
@@ -2675,14 +2701,14 @@ __device__ __forceinline__ void stage_children(const ChildRec* __restrict__ crec
 // keeps the live state small.
 // STAGED: smem is 128-byte aligned and holds [tables | child 0's footprint | child 1's], which
 // stage_children's copies fill (completion on the mbarrier at shared address bar).  Each warp
-// waits for them (bounded); a warp whose wait runs out counts a timeout and gathers from the
-// child images instead, and the tile waits once more before it ends, so that no copy into its
-// shared memory is still in flight when the CTA exits.
+// waits for them, at most wait_ns; a warp whose wait runs out counts a timeout and gathers from
+// the child images instead (the same values), and waits once more, as long, before the CTA ends,
+// so that no copy into its shared memory is still in flight when it exits.
 template <bool COHERENT = false, int THREADS = kThreads, bool STAGED = false>
 __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict__ nodes, const TileItem it,
                                            const float4* __restrict__ tables, const ChildRec* __restrict__ crec,
                                            ChildDup* C, float2* __restrict__ arena, float2* root_out, int root,
-                                           char* smem, unsigned bar = 0) {
+                                           char* smem, unsigned bar = 0, unsigned long long wait_ns = 0) {
     Job J;
     J.g = nodes[it.node];
     J.lc = J.g.tile_lc;
@@ -2695,7 +2721,7 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
     const float2* sbox[2] = {nullptr, nullptr};
     bool waited = true;
     if (STAGED && (C[0].xw > 0 || C[1].xw > 0)) {
-        waited = __all_sync(0xffffffffu, bulk_wait(bar, 0));
+        waited = __all_sync(0xffffffffu, timed_wait(bar, 0, wait_ns));
         if (!waited) {
             if ((threadIdx.x & 31) == 0) atomicAdd(&g_wait_timeouts, 1);
         } else {
@@ -2743,7 +2769,7 @@ __device__ __forceinline__ void merge_tile(float Kf, const PolarDesc* __restrict
             }
         }
     }
-    if (STAGED && !waited) bulk_wait(bar, 0);  // the copies may still land: not past the CTA's end
+    if (STAGED && !waited) timed_wait(bar, 0, wait_ns);  // the copies may still land: not past the CTA's end
 }
 
 __global__ void __launch_bounds__(kMergeThreads, 8) split_merge_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
@@ -2767,7 +2793,8 @@ __global__ void __launch_bounds__(kMergeThreads, 8) split_merge_staged_kernel(Sp
                                                                          const float4* __restrict__ tables,
                                                                          const ChildRec* __restrict__ crecs,
                                                                          float2* __restrict__ arena,
-                                                                         float2* root_out, int root) {
+                                                                         float2* root_out, int root,
+                                                                         unsigned long long wait_ns, int withheld) {
     extern __shared__ __align__(128) char smem_raw[];
     __shared__ ChildDup C[2];
     __shared__ __align__(8) unsigned long long mbar;
@@ -2775,9 +2802,10 @@ __global__ void __launch_bounds__(kMergeThreads, 8) split_merge_staged_kernel(Sp
     char* smem = smem_raw + (((raw + 127u) & ~127u) - raw);
     const unsigned bar = (unsigned)__cvta_generic_to_shared(&mbar);
     const ChildRec* crec = crecs + 2 * (long long)blockIdx.x;
-    if (threadIdx.x == 0) stage_children(crec, (unsigned)__cvta_generic_to_shared(smem + kTabBytes), bar);
-    merge_tile<false, kMergeThreads, true>(P.Kf, nodes, items[blockIdx.x], tables, crec, C, arena, root_out, root,
-                                           smem, bar);
+    const TileItem it = items[blockIdx.x];
+    if (threadIdx.x == 0)
+        stage_children(crec, (unsigned)__cvta_generic_to_shared(smem + kTabBytes), bar, it.node == withheld ? 16u : 0u);
+    merge_tile<false, kMergeThreads, true>(P.Kf, nodes, it, tables, crec, C, arena, root_out, root, smem, bar, wait_ns);
 }
 
 // All merge levels in one persistent launch.  Items are in height order; a CTA claims the next
@@ -2791,11 +2819,6 @@ __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
     return v;
 }
 
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __global__ void __launch_bounds__(kThreads, 4) split_merge_queue_kernel(SplitParams P, const PolarDesc* __restrict__ nodes,
                                                                         const TileItem* __restrict__ items, int nitems,
@@ -3116,7 +3139,7 @@ int launch_split_ffbp_leaves(const PulseInputs& in, const PolarDesc* nodes, cons
 
 int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* items, int nitems,
                              const float4* tables, const void* crecs, float2* arena, float2* root_out, int root,
-                             size_t box_bytes, cudaStream_t s) {
+                             size_t box_bytes, unsigned long long wait_ns, int withheld, cudaStream_t s) {
     if (nitems <= 0) return SARBP_OK;
     PulseInputs none{};
     none.k = k;
@@ -3126,7 +3149,7 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
         const size_t smem = 128 + kTabBytes + box_bytes;
         if (int st = prepare(split_merge_staged_kernel, smem)) return st;
         split_merge_staged_kernel<<<nitems, kMergeThreads, smem, s>>>(
-            P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs), arena, root_out, root);
+            P, nodes, items, tables, reinterpret_cast<const ChildRec*>(crecs), arena, root_out, root, wait_ns, withheld);
         note_launches(1);
         return check_launch("split_ffbp_merges (staged)");
     }

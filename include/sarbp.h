@@ -354,10 +354,13 @@ int sarbp_ffbp_set_staging(sarbp_ffbp_plan* plan, int on);
 /* *staged = 1 if the bound plan's merges stage their footprints (staging requested and the
  * driver's tensor-map encoder available at bind), else 0.  No counterpart in the reference. */
 int sarbp_ffbp_staging(const sarbp_ffbp_plan* plan, int* staged);
-/* The queue's wait limit per merge tile (default 5 s; (0, 60]) and, for tests of that limit, a merge
- * node whose children are never counted complete (withheld_node >= 0; -1 for none), so that its
- * tiles' waits run out.  Set before sarbp_ffbp_bind.  A wait that runs out stops the launch and sets
- * the status read by sarbp_ffbp_status; the image is then incomplete. */
+/* The merges' wait limit per tile (default 5 s; (0, 60]) and, for tests of that limit, a merge node
+ * whose waits run out (withheld_node >= 0; -1 for none).  Set before sarbp_ffbp_bind.  With the merge
+ * queue, the withheld node's children are never counted complete; a wait that runs out stops the
+ * launch and sets the status read by sarbp_ffbp_status, and the image is then incomplete.  With
+ * staged merges (sarbp_ffbp_set_staging), the withheld node's tiles declare more bytes than their
+ * TMA copies deliver; a warp whose wait runs out gathers from the child images instead, so the
+ * image stays the same, and sarbp_wait_timeouts counts the wait. */
 int sarbp_ffbp_set_wait_limit(sarbp_ffbp_plan* plan, double seconds, int withheld_node);
 /* *status = 1 if a merge-queue wait ran out in the last execute, else 0 (synchronises the device). */
 int sarbp_ffbp_status(const sarbp_ffbp_plan* plan, int* status);

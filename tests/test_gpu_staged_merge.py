@@ -64,3 +64,54 @@ def test_staged_merge_equals_gathered_merge_c1(lib):
     out = _images("c1")
     assert torch.equal(out[True], out[False])
     assert _timeouts(lib) == before
+
+
+def test_a_staged_wait_that_runs_out_falls_back_to_the_child_images(lib):
+    """The root's merge tiles declare 16 bytes more than their TMA copies deliver (the withheld node
+    of sarbp_ffbp_set_wait_limit), so every root warp's wait runs out after 5 ms: those warps gather
+    from the child images instead, the image is the same bit for bit, the waits are counted, and the
+    GPU stays usable."""
+    import time
+    from bp_project_gb300 import core, scenes
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    cfg = scenes.scaled(scenes.CONFIGS["c1"], pulses=1024, samples=4096, image_side=512)
+    sc = scenes.synthesize(cfg, device="cuda")
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (sc.data, sc.position, sc.weight, sc.phase)]
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split", staging=False)
+    want = prog.execute(*dev, sc.range_start, sc.data_dr, sc.k)
+    torch.cuda.synchronize()
+    prog.close()
+
+    h = lib.load()
+    arr = core.node_array(plan.nodes())
+    handle = ctypes.c_void_p()
+    crop = (plan.crop_r[0], plan.crop_u[0], plan.crop_r[1] - plan.crop_r[0], plan.crop_u[1] - plan.crop_u[0])
+    lib.check(h.sarbp_ffbp_plan_create(arr, len(arr), *crop, lib.mode_id("split"), ctypes.byref(handle)))
+    try:
+        lib.check(h.sarbp_ffbp_set_wait_limit(handle, 0.005, 0))
+        ws = torch.empty(h.sarbp_ffbp_workspace_bytes(handle), dtype=torch.uint8, device="cuda")
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        lib.check(h.sarbp_ffbp_bind(handle, ctypes.c_void_p(ws.data_ptr()), ws.numel(), stream))
+        staged = ctypes.c_int(0)
+        lib.check(h.sarbp_ffbp_staging(handle, ctypes.byref(staged)))
+        assert staged.value == 1
+        before = _timeouts(lib)
+        got = torch.zeros_like(want)
+        p, s = dev[0].shape
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+        t0 = time.perf_counter()
+        lib.check(h.sarbp_ffbp_execute(handle, ptr(dev[0]), p, s, ptr(dev[1]), ptr(dev[2]), ptr(dev[3]),
+                                       sc.range_start, sc.data_dr, sc.k, ptr(got), stream))
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+        counted = _timeouts(lib) - before
+    finally:
+        h.sarbp_ffbp_plan_destroy(handle)
+    assert counted > 0
+    assert elapsed < 10.0
+    assert torch.equal(got, want)
+    # the GPU keeps working: a plain staged plan forms the same image with no wait running out
+    out = _images("c1", pulses=1024, samples=4096, image_side=512)
+    assert torch.equal(out[True], out[False])
