@@ -1106,6 +1106,34 @@ __device__ __forceinline__ bool bulk_stage_windows(const SplitParams& P, TileSha
 }
 #endif
 
+// Horner windows of one pulse (cnt entries from bin b0) staged by one warp with one global load
+// per lane and step: lane l loads sample b0 + j0 + l - 1, and entry j0 + l (l < 29) takes its four
+// taps from lanes l .. l + 3 by shuffles (the FFBP leaves; the direct kernels' staging measured
+// the same either way).
+__device__ __forceinline__ void stage_window_shfl(const float2* __restrict__ row, long long samples, long long b0,
+                                                  int cnt, float a, float4* __restrict__ wentry, int lane) {
+    for (int j0 = 0; j0 < cnt; j0 += 29) {
+        const long long gi = b0 + j0 + lane - 1;
+        float2 x = make_float2(0.0f, 0.0f);
+        if (gi >= 0 && gi < samples) x = __ldg(row + gi);
+        float2 x1, x2, x3;
+        x1.x = __shfl_down_sync(0xffffffffu, x.x, 1);
+        x1.y = __shfl_down_sync(0xffffffffu, x.y, 1);
+        x2.x = __shfl_down_sync(0xffffffffu, x.x, 2);
+        x2.y = __shfl_down_sync(0xffffffffu, x.y, 2);
+        x3.x = __shfl_down_sync(0xffffffffu, x.x, 3);
+        x3.y = __shfl_down_sync(0xffffffffu, x.y, 3);
+        const int j = j0 + lane;
+        if (lane < 29 && j < cnt) {
+            const long long g = b0 + j;
+            float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
+            if (g >= 1 && g <= samples - 3) cubic_coefficients(x, x1, x2, x3, a, c01, c23);
+            wentry[2 * j] = c01;
+            wentry[2 * j + 1] = c23;
+        }
+    }
+}
+
 // Chunk driver shared by the forward and adjoint kernels: per chunk of up to 64
 // pulses, warps 0 and 1 compute the (tile, pulse) records (one pulse per lane, two-float,
 // on two SM sub-partitions at once) and pack the pulses' range windows, all warps
@@ -2170,15 +2198,7 @@ __device__ __forceinline__ void leaf_tile(const SplitParams& P, const PolarDesc*
                 const long long b0 = s_base[nl];
                 const float a = s_wt[nl];
                 const float2* row = in.data + (size_t)(c0 + nl) * in.samples;
-                for (int jj = lane; jj < cnt; jj += 32) {
-                    const long long gb = b0 + jj;
-                    float4 c01 = make_float4(0.f, 0.f, 0.f, 0.f), c23 = c01;
-                    if (gb >= 1 && gb <= (long long)in.samples - 3)
-                        cubic_coefficients(__ldg(row + gb - 1), __ldg(row + gb), __ldg(row + gb + 1), __ldg(row + gb + 2),
-                                           a, c01, c23);
-                    win[2 * (off + jj)] = c01;
-                    win[2 * (off + jj) + 1] = c23;
-                }
+                stage_window_shfl(row, in.samples, b0, cnt, a, win + 2 * off, lane);
             }
         }
         __syncthreads();
