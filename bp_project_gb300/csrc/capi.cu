@@ -154,10 +154,12 @@ void child_bins(const PolarDesc& p, const PolarDesc& c, int i, int j, double& qr
 
 // Footprint boxes of split-mode merges (PolarDesc::box_*, PolarDesc of each child): the child
 // stencil rows and columns that a parent tile reads, relative to the stencil bin of the tile's
-// centre pixel, over the corners and edge midpoints of up to 16 x 16 tiles of each parent
-// (evenly spaced, the first and last included), plus one bin of margin on every side.  The
-// mapping is smooth over a tile, so the sampled extremes bound the rest up to that margin; a
-// warp whose stencils fall outside the staged box reads the child image instead.  A box over
+// centre pixel, over the corners and edge midpoints of up to 4 x 4 tiles of each parent (evenly
+// spaced, the first and last included), plus one bin of margin on every side.  The mapping is
+// smooth and the footprints grow monotonically towards the grid's edges, so the sampled extremes
+// bound the rest up to that margin; a warp whose stencils fall outside the staged box reads the
+// child image instead.  (Plans are rebuilt per autofocus iteration: this stays well under a
+// millisecond for them.)  A box over
 // 256 rows or columns (the TMA's limit) or kMaxChildBox bytes is not staged.  Also sets
 // merge_box_bytes per height.
 void child_footprints(sarbp_ffbp_plan& p) {
@@ -167,7 +169,7 @@ void child_footprints(sarbp_ffbp_plan& p) {
         if (d.left < 0) continue;
         const int cols_t = 1 << d.tile_lc, rows_t = kSplitTilePixels >> d.tile_lc;
         const int ntr = (d.win_nr + rows_t - 1) / rows_t, ntu = (d.win_nu + cols_t - 1) / cols_t;
-        const int sr = std::min(ntr, 16), su = std::min(ntu, 16);
+        const int sr = std::min(ntr, 4), su = std::min(ntu, 4);
         size_t bytes = 0;
         for (int ch : {d.left, d.right}) {
             PolarDesc& c = p.nodes[ch];
