@@ -295,7 +295,10 @@ int launch_split_ffbp_merges(double k, const PolarDesc* nodes, const TileItem* i
 __host__ __device__ inline size_t split_box_bytes(int rows, int cols) { return ((size_t)rows * cols * 8 + 127) / 128 * 128; }
 // Largest staged footprint per child: with two of them, the tables, the alignment slack and the
 // static shared memory a merge CTA stays within 28 KB, so eight fit an SM's 228 KB.
-constexpr size_t kMaxChildBox = 9728;
+#ifndef SARBP_XP_MAXBOX
+#define SARBP_XP_MAXBOX 9728
+#endif
+constexpr size_t kMaxChildBox = SARBP_XP_MAXBOX;
 // Tensor-map bytes per node.
 constexpr size_t kTensorMapBytes = 128;
 
