@@ -159,9 +159,8 @@ void child_bins(const PolarDesc& p, const PolarDesc& c, int i, int j, double& qr
 // smooth and the footprints grow monotonically towards the grid's edges, so the sampled extremes
 // bound the rest up to that margin; a warp whose stencils fall outside the staged box reads the
 // child image instead.  (Plans are rebuilt per autofocus iteration: this stays well under a
-// millisecond for them.)  A box over
-// 256 rows or columns (the TMA's limit) or kMaxChildBox bytes is not staged.  Also sets
-// merge_box_bytes per height.
+// millisecond for them.)  A box over 256 rows or columns (the TMA's limit) or kMaxChildBox bytes
+// is not staged.  Also sets merge_box_bytes per height.
 void child_footprints(sarbp_ffbp_plan& p) {
     p.merge_box_bytes.assign(p.max_height + 1, 0);
     for (int n = 0; n < p.n_nodes; ++n) {
@@ -206,8 +205,10 @@ void child_footprints(sarbp_ffbp_plan& p) {
             c.box_w = 0;
             if (!finite || lo_r + hi_r > 250.0 || lo_u + hi_u > 250.0) continue;
             const int br = (int)lo_r + 1, bu = (int)lo_u + 1;
-            const int bh = std::max(br + (int)hi_r + 1 + 1, 8);       // the kernel's box tests need >= 5 x 4
-            int bw = std::max(bu + (int)hi_u + 1 + 2, 8);  // +1: the first column is rounded down to an even one
+            // At least 8 x 8 (the kernel's block test needs 5 x 4); one more column because the
+            // first one is rounded down to an even column.
+            const int bh = std::max(br + (int)hi_r + 1 + 1, 8);
+            int bw = std::max(bu + (int)hi_u + 1 + 2, 8);
             bw += bw & 1;
             if (bh > 256 || bw > 256 || split_box_bytes(bh, bw) > kMaxChildBox) continue;
             c.box_r = br;
