@@ -112,11 +112,19 @@ def test_ffbp_plan_object_on_host(golden, lib, mode):
         assert h.sarbp_ffbp_set_wait_limit(handle, 0.0, -1) == lib.SARBP_ERR_VALUE
         assert h.sarbp_ffbp_set_wait_limit(handle, 1.0, len(arr) - 1) == lib.SARBP_ERR_VALUE  # a leaf
         assert h.sarbp_ffbp_set_wait_limit(handle, 1.0, 0) == 0
+        # merge-tile staging: on by default, switchable before bind; nothing staged until bound
+        assert h.sarbp_ffbp_set_staging(handle, 2) == lib.SARBP_ERR_VALUE
+        assert h.sarbp_ffbp_set_staging(handle, 0) == 0
+        assert h.sarbp_ffbp_set_staging(handle, 1) == 0
+        staged = ctypes.c_int(-1)
+        assert h.sarbp_ffbp_staging(handle, ctypes.byref(staged)) == 0 and staged.value == 0
+        assert h.sarbp_ffbp_staging(handle, None) == lib.SARBP_ERR_TYPE
     else:
         assert h.sarbp_ffbp_set_merge_queue(handle, 1) == lib.SARBP_ERR_VALUE
     ws = h.sarbp_ffbp_workspace_bytes(handle)
+    # node images (split mode: rows padded to an even length) + tables, tile records, node list
     images = sum(n.nr * n.nu * 8 for n in plan.nodes()[1:])
-    assert images <= ws <= images * 1.06 + (1 << 26)  # + tables, tile records, node list
+    assert images <= ws <= images * 1.06 + (1 << 26)
     # binding without a workspace is refused on the host
     assert h.sarbp_ffbp_bind(handle, None, 0, None) == lib.SARBP_ERR_WORKSPACE
     h.sarbp_ffbp_plan_destroy(handle)
