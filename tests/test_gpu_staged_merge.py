@@ -24,7 +24,8 @@ def lib():
 def _images(config, **scale):
     from bp_project_gb300 import core, scenes
     from bp_project_gb300.gpu_backend import build_ffbp_plan
-    cfg = scenes.scaled(scenes.CONFIGS[config], **scale) if scale else scenes.CONFIGS[config]
+    base = scenes.batch_configs(64)[int(config[5:])][0] if config.startswith("batch") else scenes.CONFIGS[config]
+    cfg = scenes.scaled(base, **scale) if scale else base
     sc = scenes.synthesize(cfg, device="cuda")
     plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
                            range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
@@ -46,9 +47,13 @@ def _timeouts(lib):
     return n.value
 
 
+# c1 and c2 geometries (32 x 32 and 16 x 64 merge tiles, boxes under 9.5 KB per child), the c0 scene, and
+# a 7.7 km scene of the batch workload whose lowest merge levels run on 8 x 128 tiles with boxes of about
+# 12.9 KB per child (six CTAs per SM)
 @pytest.mark.parametrize("config,scale", [("c1", dict(pulses=1024, samples=4096, image_side=512)),
                                           ("c2", dict(pulses=2048, samples=4096, image_side=512)),
-                                          ("c0", {})])
+                                          ("c0", {}),
+                                          ("batch6", dict(pulses=1024))])
 def test_staged_merge_equals_gathered_merge(lib, config, scale):
     before = _timeouts(lib)
     out = _images(config, **scale)
