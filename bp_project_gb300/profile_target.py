@@ -9,7 +9,8 @@ its kernels:
 Workloads: ``direct`` (split-precision direct BP on the scene's ground
 lattice), ``polar`` (split-precision direct BP onto a 1024 x 4096 window of the
 scene's FFBP root polar grid, the ``CudaBaseline.run_direct`` surface),
-``ffbp`` (level-batched FFBP + split evaluation onto the lattice),
+``ffbp`` (level-batched FFBP + split evaluation onto the lattice; ``--no-staging``: merge tiles
+gather from the child images instead of staging their footprints by TMA),
 ``plain`` (the FP64-phase mixed kernel on a 64-row band of the lattice),
 ``adjoint`` (forward + adjoint of lattice BP, the entropy autofocus step),
 ``range`` (range compression of the scene's data treated as raw echoes),
@@ -97,6 +98,8 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--mode", default="split")
     ap.add_argument("--warmups", type=int, default=0, help="untimed repetitions before the profiled range")
+    ap.add_argument("--no-staging", action="store_true",
+                    help="ffbp: merge tiles gather from the child images instead of staging their footprints by TMA")
     args = ap.parse_args(argv)
     build.build()
     torch.cuda.set_device(0)
@@ -180,7 +183,8 @@ def main(argv=None):
     else:
         plan = build_ffbp_plan(scene.position, cfg.fc, scene.extent, side=1, leaf_size=cfg.leaf_size,
                                range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
-        prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode=args.mode, device=dev)
+        prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode=args.mode, device=dev,
+                                staging=not args.no_staging)
         ground = torch.empty((lat.rows, lat.cols), dtype=torch.complex64, device=dev)
         grid = plan.grid()
 
