@@ -120,3 +120,30 @@ def test_a_staged_wait_that_runs_out_falls_back_to_the_child_images(lib):
     # the GPU keeps working: a plain staged plan forms the same image with no wait running out
     out = _images("c1", pulses=1024, samples=4096, image_side=512)
     assert torch.equal(out[True], out[False])
+
+
+def test_far_range_ffbp_vs_reference_ffbp(lib):
+    """A 7.7 km scene of the uneven batch workload (1024 pulses onto 256² at 0.5 m), whose lowest merge
+    levels stage 12.9 KB footprints: split FFBP within 1e-4 of the reference FFBP (oracle restatement of
+    ffbp.form_ffbp on the same plan), with the same peak pixel."""
+    from bp_project_gb300 import core, scenes
+    from bp_project_gb300.gpu_backend import build_ffbp_plan
+    from conftest import rel_err
+    from oracle import reference as ora
+    cfg = scenes.scaled(scenes.batch_configs(64)[6][0], pulses=1024)
+    sc = scenes.synthesize(cfg, device="cuda")
+    plan = build_ffbp_plan(sc.position, cfg.fc, sc.extent, side=1, leaf_size=cfg.leaf_size,
+                           range_spacing=cfg.range_spacing, angular_oversample=cfg.angular_oversample)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (sc.data, sc.position, sc.weight, sc.phase)]
+    prog = core.FFBPProgram(plan.nodes(), plan.crop_r, plan.crop_u, mode="split")
+    assert prog.staged
+    img = prog.execute(*dev, sc.range_start, sc.data_dr, sc.k).cpu().numpy()
+    prog.close()
+    ref, _ = ora.form_ffbp(sc.data, sc.position, sc.range_start, sc.data_dr, cfg.fc, sc.extent, side=1,
+                           leaf_size=cfg.leaf_size, range_spacing=cfg.range_spacing,
+                           angular_oversample=cfg.angular_oversample, weight=sc.weight, phase=sc.phase)
+    err = rel_err(ref.image, img)
+    print(f"far-range split FFBP vs reference FFBP: {err:.3e}")
+    assert err <= 1e-4
+    assert np.unravel_index(np.abs(img).argmax(), img.shape) == np.unravel_index(np.abs(ref.image).argmax(),
+                                                                                   ref.image.shape)
