@@ -26,5 +26,6 @@ class BatchedResidentProgram(ResidentProgram):
             "extra_table_bytes": 0,
             "extra_table_count": 0,
             "batch_mapping": "one CTA per node pixel tile; nodes grouped by subtree height",
-            "fusion": "leaf BP per tile; each parent child regrid rounded to complex64 then FP32 add",
+            "fusion": "leaf BP per tile; each merge tile regrids both children (footprints staged in shared memory "
+                      "by TMA in split mode), each rounded to complex64, then an FP32 add",
         })

@@ -91,6 +91,8 @@ class ResidentProgram:
             "graph_error": None,
             "arithmetic": "libsarbp sm_103a kernels; split = split precision, others = reference policies",
             "fusion": "level-batched; child regrids rounded to complex64 then FP32 add" if algorithm == "ffbp" else None,
+            "merge_staging": ("TMA tensor copies of each child's footprint into shared memory"
+                              if self._ffbp is not None and self._ffbp.staged else None),
         }
 
     def execute(self):
